@@ -1,0 +1,202 @@
+/*
+ * nbg.h -- C ABI of the GB300 spiking-network step engine.
+ *
+ * This is the boundary the reference's C++ host (and its pybind11 module)
+ * calls instead of the legacy per-model GPU interfaces and the dense runtime.
+ * Plain C types only: no torch, no C++ objects cross it.  Every entry point
+ * returns an nbg_status; nbg_last_error() gives a readable reason for the
+ * last failure on the calling thread (the reference reports reasons through
+ * `bool + std::string* reason`, e.g. src/native/gpu/src/gpu_runtime/
+ * GpuPropagationRuntime.cu:19-29).
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   nbg_create      Simulation::Simulation(NeuronLayerDescription...,
+ *                   ConnectionDescription..., LearningRuleDescription...)
+ *                   src/native/legacy/source_file_realtime_v1_async/
+ *                   Simulation/inc/Simulation.h:187-250, and the network
+ *                   compile Network::CaculateOutputConnection /
+ *                   CaculateInputConnection (Network/src/Network.cu:483-735)
+ *   nbg_run         Simulation::RunSimulationStep(int) (Simulation.h:182,
+ *                   Simulation/src/Simulation.cu:383-474) together with the
+ *                   CoreCuda per-model UpdateState launches
+ *                   (TimeDrivenLIF_Voltage_jump_GPU_Interface.cu:70-104) and
+ *                   DenseSubnetworkRuntimeGpu::RunStep
+ *                   (src/native/gpu/src/dense_subnetwork/
+ *                   DenseSubnetworkRuntimeGpu.cpp:625-665)
+ *   nbg_get_state   the per-neuron state read of _core.Simulation.neuron_state
+ *                   (python/bindings/neuronbridge_core.cpp:940-975)
+ *   nbg_get_spikes  _core.Simulation.output_spikes (neuronbridge_core.cpp:490-508)
+ *   nbg_get_weights / nbg_set_weight
+ *                   Simulation::Get/SetConnectionWeight (Simulation.h:367-373)
+ *   nbg_reset       Simulation::ResetForNextRound
+ */
+#ifndef NBG_H
+#define NBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int nbg_status;
+enum {
+    NBG_OK = 0,
+    NBG_ERR_INVALID = 1,  /* bad argument or network description */
+    NBG_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    NBG_ERR_OOM = 3,      /* device allocation failed */
+    NBG_ERR_OVERFLOW = 4, /* a recording buffer filled up */
+    NBG_ERR_STATE = 5,    /* call not valid in the engine's current state */
+    NBG_ERR_TIMEOUT = 6,  /* a bounded device wait gave up */
+    NBG_ERR_UNSUPPORTED = 7
+};
+
+/* Neuron models (catalog names in parentheses, aliases as in the reference's
+ * src/native/shared/src/neuron_model/NeuronModelCatalog.cpp:60-200). */
+enum {
+    NBG_MODEL_LIF_VJ = 0,   /* TimeDrivenLIF_Voltage_jump[_GPU] */
+    NBG_MODEL_IZH_COND = 1, /* TimeDrivenIzhikevic_[I_]Exponential_Decay[_GPU] */
+    NBG_MODEL_IZH_RK4 = 2,  /* IzhikevichCurrentRK4: current pulses, noise, RK4 */
+    NBG_MODEL_POISSON = 3   /* PoissonRate[_GPU] */
+};
+
+/* Semantics profile: LEGACY_CPU is the parity target (strict '>' LIF
+ * threshold, refractory-gated arrivals); DENSE follows the reference's dense
+ * GPU runtime for the voltage-jump LIF ('>=' threshold, ungated arrivals,
+ * v starts at V_rest). */
+enum { NBG_SEM_LEGACY_CPU = 0, NBG_SEM_DENSE = 1 };
+
+#define NBG_NFP 16
+#define NBG_NIP 4
+
+/* Per-layer parameters.  Slot meaning by model:
+ *  LIF_VJ:   f[0] V_rest, f[1] tau, f[2] V_th, f[3] R, f[4] V_reset,
+ *            f[5] random_mu[0], f[6] I_ext;          ip[0] t_ref (steps)
+ *  IZH_COND: f[0] a, f[1] b, f[2] c, f[3] d, f[4] V_rest, f[5] V_th, f[6] R,
+ *            f[7] E_ampa, f[8] ampa_tau, f[9] E_gaba, f[10] gaba_tau,
+ *            f[11] I_ext
+ *  IZH_RK4:  f[0] a, f[1] b, f[2] c, f[3] d, f[4] v0, f[5] V_th,
+ *            f[6] noise sigma, f[7] I_bias
+ *  POISSON:  f[0] rate_bias_hz, f[1] rate_gain_hz_per_current, f[2] I_ext */
+typedef struct {
+    int model;
+    int count;
+    float f[NBG_NFP];
+    int ip[NBG_NIP];
+} nbg_layer_desc;
+
+/* Pair STDP parameters (STDP::SetParameters keys Max_LTP, LTP_tau, Max_LTD,
+ * LTD_tau; src/native/legacy/.../LearningRule/src/Rule/STDP.cpp:63-87). */
+typedef struct {
+    float max_ltp, ltp_tau, max_ltd, ltd_tau;
+} nbg_stdp_desc;
+
+/* Network description: layers in creation order (global neuron ids are
+ * assigned layer by layer), then connections as parallel arrays in original
+ * connection order (the reference's ConnectionDescription,
+ * Network/inc/NetworkConstructStructure.h:18-74).  type 0 = excitatory,
+ * 1 = inhibitory; delay in steps (>= 1); rule = index into rules or -1. */
+typedef struct {
+    int n_layers;
+    const nbg_layer_desc *layers;
+    int64_t n_conn;
+    const int32_t *source;
+    const int32_t *target;
+    const int32_t *type;
+    const float *weight;
+    const float *max_weight;
+    const int32_t *delay;
+    const int32_t *rule;
+    int n_rules;
+    const nbg_stdp_desc *rules;
+    float dt_ms;
+    int semantics;
+    uint64_t seed; /* noise seed for IZH_RK4 layers */
+} nbg_net_desc;
+
+/* Engine options (no reference counterpart; the reference's SimulationConfig
+ * queues/event_queue have no meaning on the device). */
+typedef struct {
+    int device;            /* CUDA device ordinal */
+    int block_steps;       /* max steps per update launch (0 = auto: min delay) */
+    int threads_per_block; /* 0 = auto */
+    int64_t spike_capacity;/* device raster capacity per run call (0 = auto) */
+    int use_graph;         /* capture the per-block launches in a CUDA graph */
+    int64_t event_log_capacity; /* >0: log delivered events (testing aid) */
+    int kernel_timing;     /* bracket every launch with CUDA events (nbg_profile) */
+} nbg_options;
+
+typedef struct nbg_engine nbg_engine;
+
+const char *nbg_last_error(void);
+const char *nbg_version(void);
+
+void nbg_default_options(nbg_options *opt);
+nbg_status nbg_create(const nbg_net_desc *desc, const nbg_options *opt, nbg_engine **out);
+nbg_status nbg_destroy(nbg_engine *e);
+
+/* Advance the network.  The first call performs steps+1 updates (t=0..steps),
+ * later calls perform `steps` updates, matching the reference's run(). */
+nbg_status nbg_run(nbg_engine *e, int steps);
+nbg_status nbg_reset(nbg_engine *e);
+nbg_status nbg_next_time(const nbg_engine *e, int *t);
+nbg_status nbg_num_neurons(const nbg_engine *e, int *n);
+nbg_status nbg_num_synapses(const nbg_engine *e, int64_t *s);
+/* minimum delay over synapses (the temporal-blocking window) */
+nbg_status nbg_block_steps(const nbg_engine *e, int *b);
+
+/* State fields for nbg_get_state / nbg_set_state. */
+enum {
+    NBG_FIELD_V = 0,
+    NBG_FIELD_U = 1,
+    NBG_FIELD_G_EXC = 2,
+    NBG_FIELD_G_INH = 3,
+    NBG_FIELD_I_EXT = 4,
+    NBG_FIELD_LAST_SPIKE = 6 /* written as float */
+};
+nbg_status nbg_get_state(nbg_engine *e, int field, float *out /* n_neurons */);
+nbg_status nbg_set_state(nbg_engine *e, int field, const float *in /* n_neurons */);
+
+/* Spikes recorded by all run calls so far, ordered by (time, neuron id). */
+nbg_status nbg_num_spikes(nbg_engine *e, int64_t *n);
+nbg_status nbg_get_spikes(nbg_engine *e, int32_t *times, int32_t *ids, int64_t capacity);
+nbg_status nbg_clear_spikes(nbg_engine *e);
+/* delivered synaptic events accumulated over all run calls */
+nbg_status nbg_num_events(nbg_engine *e, int64_t *n);
+
+/* Weights and STDP state in original connection order. */
+nbg_status nbg_get_weights(nbg_engine *e, float *w, float *apre, float *apost, int32_t *last);
+nbg_status nbg_set_weight(nbg_engine *e, int64_t conn, float w);
+
+/* Set neuron `id`'s external current to `value` at the start of step t
+ * (before that step's arrivals), as a delay-d current connection from an
+ * input-current neuron does in the reference (ProcessCurrent sets the
+ * target's total current, e.g. TimeDrivenLIF_Voltage_jump.cpp:117-124;
+ * PROPOGATEDCURRENT outranks PROPOGATEDSPIKE, Event.h:10). */
+nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value);
+
+/* Membrane (field 0) traces of selected neurons, one row per update. */
+nbg_status nbg_set_trace(nbg_engine *e, int n, const int32_t *ids);
+nbg_status nbg_num_trace_rows(nbg_engine *e, int64_t *rows);
+nbg_status nbg_get_traces(nbg_engine *e, float *out /* rows * n */);
+
+/* Delivered-event log (testing aid, enabled by options.event_log_capacity):
+ * (time, original connection index, delivered weight). */
+nbg_status nbg_num_logged_events(nbg_engine *e, int64_t *n);
+nbg_status nbg_get_logged_events(nbg_engine *e, int32_t *t, int64_t *conn, float *w);
+
+/* Device timings of the last run call, from CUDA events on the engine's
+ * stream: total_ms spans all launches of the call; with options.kernel_timing
+ * update_ms / propagate_ms sum the per-launch durations of the update (drain
+ * + neuron step) and spike-propagation kernels (else 0).  launches counts the
+ * kernels launched.  Mirrors the phase split of the reference's
+ * bench_profiling_snapshot (neuronbridge_core.cpp:1887). */
+nbg_status nbg_profile(nbg_engine *e, double *total_ms, double *update_ms, double *propagate_ms,
+                       int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBG_H */

@@ -1,0 +1,1344 @@
+// nbg_engine.cu -- GB300 (sm_103a) step engine for NeuronBridge's time-driven
+// spiking networks: network compile on the host, two kernels per block of
+// steps on the device, C ABI in include/nbg.h.
+//
+// Execution model (owner computes by target neuron):
+//   * Every synapse has a bit in a per-step "arrival mask" ring:
+//       mask[slot][woff[j] + p/32] bit p%32   for in-synapse p of target j
+//     (p is the synapse's rank in j's CSC list, sorted by source id).
+//   * k_update: one thread per target neuron advances it `B` steps.  At each
+//     step it reads its own mask words for slot t % D, applies the marked
+//     arrivals in ascending CSC order (the canonical order of the oracle),
+//     runs the pre-synaptic STDP hook of each plastic arrival, integrates the
+//     neuron, and on a spike runs the post-synaptic STDP pass over its own
+//     CSC list.  Spikes are compacted per step with a warp ballot.
+//   * k_propagate: for every spike of the block, every out-synapse (CSR by
+//     source) sets its bit in slot (t + delay) % D with atomicOr.  OR is
+//     commutative, so the mask -- and therefore every later sum -- does not
+//     depend on the order in which threads run: results are bit-exact and
+//     reproducible without floating-point atomics.
+//   * Temporal blocking: a spike at t reaches its targets at t + d >= t + dmin,
+//     so B = dmin steps can be advanced per target with no global exchange.
+//
+// Reference counterparts (paths inside the reference project):
+//   LIF update     .../NeuralModel/src/TimeDriven/TimeDrivenLIF_Voltage_jump.cpp:49-113
+//                  .../Intergration/inc/FixStep/ForwardEulerMethod.h:29-55
+//   Izhikevich     .../TimeDrivenIzhikevic_Exponential_Decay.cpp:59-131
+//   Poisson        .../TimeDriven/PoissonRate.cpp:12-22,55-78
+//   delivery       .../Event/src/Spike/PropogatedSpikeGroup.cpp:33-72,
+//                  .../Event/src/Spike/TimeDrivenInternalSpike.cpp:37-145,
+//                  src/native/gpu/src/gpu_runtime/GpuPropagationRuntime.cu:150-266
+//   STDP           .../LearningRule/src/Rule/STDP.cpp:19-61,
+//                  .../LearningRule/src/State/STDP_State.cpp:17-26
+//   dense profile  src/native/gpu/include/dense_subnetwork/model/
+//                  DenseLifVoltageJumpDeviceUpdate.cuh:10-51
+//
+// Built with -fmad=false: every float operation rounds once, as in the
+// reference's scalar C++ and the oracle (-ffp-contract=off).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/nbg.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+nbg_status fail(nbg_status code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define NBG_CUDA(call)                                                                         \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? NBG_ERR_OOM : NBG_ERR_CUDA,          \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+constexpr int kMaxBlockSteps = 32;
+constexpr int kErrOverflow = 1;
+constexpr int kErrEventLog = 2;
+
+// ---------------------------------------------------------------- device data
+
+struct LayerDev {
+    int model, start, count, has_exc, has_inh;
+    float f[NBG_NFP];
+    int ip[NBG_NIP];
+    float decay_exc, decay_inh; // IZH_COND conductance decay per step
+    float alpha;                // DENSE LIF: dt / tau
+};
+
+struct NetDev {
+    int N, D, Wt, n_layers, semantics;
+    float dt;
+    unsigned long long seed;
+    const unsigned short *pop;
+    const LayerDev *layers;
+    float *v, *u, *gexc, *ginh, *iext;
+    int *last;
+    const int *csc_ptr, *woff;
+    float *w;
+    const float *wmax;
+    const unsigned char *meta; // bit0 type, bits1..7 rule+1
+    float *apre, *apost;
+    int *slast;
+    const float *dtab; // [rule][2][dtab_len]
+    int dtab_len;
+    const float *rule_a; // [rule][2] = max_ltp, max_ltd
+    unsigned int *mask;
+    const int *out_ptr;
+    const unsigned int *out_bit;
+    const unsigned short *out_delay;
+    int *blk_spk, *blk_cnt;
+    int *out_ids, *out_cnt;
+    long long *cursor;
+    long long out_cap;
+    int *err;
+    int *tnow, *run_t0;
+    unsigned int *done;
+    const int *trace_slot;
+    float *trace;
+    int ntrace;
+    int *ev_t, *ev_pos;
+    float *ev_w;
+    unsigned long long *ev_cursor;
+    long long ev_cap;
+    unsigned long long *n_events;
+};
+
+__device__ __forceinline__ float hash_uniform01(int neuron_index, int time_step) {
+    unsigned int x = (unsigned int)neuron_index * 747796405u + (unsigned int)(time_step + 1) * 2891336453u +
+                     0x9e3779b9u;
+    x ^= x >> 16;
+    x *= 2246822519u;
+    x ^= x >> 13;
+    x *= 3266489917u;
+    x ^= x >> 16;
+    return (float)(x & 0x00FFFFFFu) / (float)0x01000000u;
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// Irwin-Hall(12) approximation of N(0,1), integer sum converted once.
+__device__ __forceinline__ float gauss12(unsigned long long seed, int neuron, int t) {
+    int m = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        unsigned long long h = mix64(seed + (unsigned long long)(unsigned int)neuron * 0x9E3779B97F4A7C15ULL +
+                                     ((unsigned long long)(unsigned int)t * 6ull + (unsigned long long)k) *
+                                         0xD1B54A32D192ED03ULL);
+        m += (int)(h & 0xFFFFFFu) + (int)((h >> 32) & 0xFFFFFFu);
+    }
+    return (float)(m - 6 * 16777216) * (1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ float izh_f(float v, float u, float I) {
+    return 0.04f * v * v + 5.0f * v + 140.0f - u + I;
+}
+__device__ __forceinline__ float izh_g(float a, float b, float v, float u) { return a * (b * v - u); }
+
+struct NeuronRegs {
+    float v, u, gexc, ginh, iext;
+    int last;
+};
+
+// STDP trace decay to time t (STDP_State::SetUpdate) from the host table.
+__device__ __forceinline__ void stdp_decay(const NetDev &n, int s, int rule, int t) {
+    int k = t - n.slast[s];
+    float fp = 0.0f, fm = 0.0f;
+    if (k < n.dtab_len) {
+        fp = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + k]);
+        fm = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + k]);
+    }
+    n.apre[s] = n.apre[s] * fp;
+    n.apost[s] = n.apost[s] * fm;
+    n.slast[s] = t;
+}
+
+__device__ __forceinline__ float clamp_w(float w, float wmax) {
+    if (w < 0.0f) return 0.0f;
+    if (w > wmax) return wmax;
+    return w;
+}
+
+// Apply one arrival (ProcessSpike of the target model), then the pre hook.
+__device__ __forceinline__ void apply_arrival(const NetDev &n, const LayerDev &L, NeuronRegs &r, float &acc_a,
+                                              float &acc_b, bool gate, int s, int t) {
+    const unsigned char meta = n.meta[s];
+    const int type = meta & 1;
+    const int rule = (int)(meta >> 1) - 1;
+    const float w = n.w[s];
+    switch (L.model) {
+    case NBG_MODEL_LIF_VJ:
+        if (n.semantics == NBG_SEM_DENSE) {
+            if (type == 0) acc_a = acc_a + w;
+            else acc_b = acc_b + w;
+        } else if (gate) {
+            r.v = r.v + (type ? -w : w);
+        }
+        break;
+    case NBG_MODEL_IZH_COND:
+        if (type == 0) r.gexc = r.gexc + w;
+        else r.ginh = r.ginh + w;
+        break;
+    default: // IZH_RK4 current pulse, POISSON rate increment
+        acc_a = acc_a + (type ? -w : w);
+        break;
+    }
+    if (n.ev_t) {
+        unsigned long long pos = atomicAdd(n.ev_cursor, 1ull);
+        if (pos < (unsigned long long)n.ev_cap) {
+            n.ev_t[pos] = t;
+            n.ev_pos[pos] = s;
+            n.ev_w[pos] = w;
+        } else {
+            atomicOr(n.err, kErrEventLog);
+        }
+    }
+    if (rule >= 0) {
+        stdp_decay(n, s, rule, t);
+        n.apre[s] = n.apre[s] + 1.0f;
+        const float am = __ldg(&n.rule_a[rule * 2 + 1]);
+        n.w[s] = clamp_w(w + (-am * n.apost[s]), n.wmax[s]);
+    }
+}
+
+// One neuron update; returns true on a spike.
+__device__ __forceinline__ bool update_neuron(const NetDev &n, const LayerDev &L, NeuronRegs &r, float acc_a,
+                                             float acc_b, int j, int t) {
+    switch (L.model) {
+    case NBG_MODEL_LIF_VJ: {
+        if (n.semantics == NBG_SEM_DENSE) {
+            float nv = r.v + acc_a - acc_b;
+            if (r.last >= L.ip[0]) nv = nv + L.alpha * (L.f[0] - nv + L.f[3] * r.iext);
+            r.last += 1;
+            if (nv >= L.f[2]) {
+                r.v = L.f[4];
+                r.last = 0;
+                return true;
+            }
+            r.v = nv;
+            return false;
+        }
+        float cur = 0.0f;
+        cur = cur + L.f[3] * r.iext / L.f[1];
+        float aux = (r.last > L.ip[0]) ? cur + (L.f[0] - r.v) / L.f[1] : 0.0f;
+        r.v = r.v + aux * n.dt;
+        r.last += 1;
+        if (r.v > L.f[2]) {
+            r.v = L.f[4];
+            r.last = 0;
+            return true;
+        }
+        return false;
+    }
+    case NBG_MODEL_IZH_COND: {
+        const float V = r.v, U = r.u;
+        float total = 0.0f;
+        if (L.has_exc) total = total + r.gexc * (L.f[7] - V);
+        if (L.has_inh) total = total + r.ginh * (L.f[9] - V);
+        total = total + r.iext;
+        float dv = 0.0f, du = 0.0f;
+        if (r.last > 0) {
+            dv = 0.04f * V * V + 5.0f * V + 140.0f - U + L.f[6] * total;
+            du = L.f[0] * (L.f[1] * V - U);
+        }
+        r.v = r.v + dv * n.dt;
+        r.u = r.u + du * n.dt;
+        if (L.has_exc) r.gexc = r.gexc * L.decay_exc;
+        if (L.has_inh) r.ginh = r.ginh * L.decay_inh;
+        r.last += 1;
+        if (r.v >= L.f[5]) {
+            r.v = L.f[2];
+            r.u = r.u + L.f[3];
+            r.last = 0;
+            return true;
+        }
+        return false;
+    }
+    case NBG_MODEL_IZH_RK4: {
+        const float a = L.f[0], b = L.f[1];
+        float I = acc_a + r.iext;
+        if (L.f[6] != 0.0f) I = I + L.f[6] * gauss12(n.seed, j, t);
+        if (r.last > 0) {
+            const float h = n.dt, hh = 0.5f * n.dt, h6 = n.dt / 6.0f;
+            const float v = r.v, u = r.u;
+            const float k1v = izh_f(v, u, I), k1u = izh_g(a, b, v, u);
+            const float v2 = v + hh * k1v, u2 = u + hh * k1u;
+            const float k2v = izh_f(v2, u2, I), k2u = izh_g(a, b, v2, u2);
+            const float v3 = v + hh * k2v, u3 = u + hh * k2u;
+            const float k3v = izh_f(v3, u3, I), k3u = izh_g(a, b, v3, u3);
+            const float v4 = v + h * k3v, u4 = u + h * k3u;
+            const float k4v = izh_f(v4, u4, I), k4u = izh_g(a, b, v4, u4);
+            r.v = v + h6 * (k1v + 2.0f * k2v + 2.0f * k3v + k4v);
+            r.u = u + h6 * (k1u + 2.0f * k2u + 2.0f * k3u + k4u);
+        }
+        r.last += 1;
+        if (r.v >= L.f[5]) {
+            r.v = L.f[2];
+            r.u = r.u + L.f[3];
+            r.last = 0;
+            return true;
+        }
+        return false;
+    }
+    default: { // POISSON
+        float rate = L.f[0] + acc_a + L.f[1] * r.iext;
+        rate = rate > 0.0f ? rate : 0.0f;
+        float prob = rate * n.dt * 0.001f;
+        prob = prob < 1.0f ? prob : 1.0f;
+        if (hash_uniform01(j - L.start, t) < prob) {
+            r.last = 0;
+            return true;
+        }
+        r.last += 1;
+        return false;
+    }
+    }
+}
+
+// Advance every neuron B steps (drain arrivals, integrate, compact spikes,
+// post-synaptic STDP).  One thread per neuron; all lanes stay in the loop so
+// the per-step warp ballot is full-warp.
+__global__ void __launch_bounds__(256) k_update(NetDev n, int B) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = j < n.N;
+    const int lane = threadIdx.x & 31;
+    const int T0 = *n.tnow;
+    const int run_t0 = *n.run_t0;
+
+    LayerDev L;
+    NeuronRegs r;
+    int base = 0, woff = 0, nw = 0, tslot = -1;
+    if (active) {
+        L = n.layers[n.pop[j]];
+        r.v = n.v[j];
+        r.u = n.u[j];
+        r.gexc = n.gexc[j];
+        r.ginh = n.ginh[j];
+        r.iext = n.iext[j];
+        r.last = n.last[j];
+        base = n.csc_ptr[j];
+        woff = n.woff[j];
+        nw = n.woff[j + 1] - woff;
+        if (n.trace_slot) tslot = n.trace_slot[j];
+    }
+    unsigned long long delivered = 0;
+    for (int b = 0; b < B; ++b) {
+        const int t = T0 + b;
+        bool spk = false;
+        if (active) {
+            float acc_a = 0.0f, acc_b = 0.0f;
+            const bool gate = r.last > L.ip[0];
+            unsigned int *mrow = n.mask + (size_t)((unsigned int)t % (unsigned int)n.D) * n.Wt + woff;
+            for (int wi = 0; wi < nw; ++wi) {
+                unsigned int word = mrow[wi];
+                if (!word) continue;
+                mrow[wi] = 0u;
+                delivered += __popc(word);
+                while (word) {
+                    const int p = wi * 32 + __ffs(word) - 1;
+                    word &= word - 1u;
+                    apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
+                }
+            }
+            spk = update_neuron(n, L, r, acc_a, acc_b, j, t);
+            if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
+        }
+        const unsigned int bal = __ballot_sync(0xffffffffu, spk);
+        if (bal) {
+            const int leader = __ffs(bal) - 1;
+            int pos = 0;
+            if (lane == leader) pos = atomicAdd(&n.blk_cnt[b], __popc(bal));
+            pos = __shfl_sync(0xffffffffu, pos, leader);
+            if (spk) {
+                n.blk_spk[(size_t)b * n.N + pos + __popc(bal & ((1u << lane) - 1u))] = j;
+                // post-synaptic STDP over this neuron's plastic in-synapses
+                const int end = n.csc_ptr[j + 1];
+                for (int s = base; s < end; ++s) {
+                    const unsigned char meta = n.meta[s];
+                    if (meta < 2) continue;
+                    const int rule = (int)(meta >> 1) - 1;
+                    stdp_decay(n, s, rule, t);
+                    n.apost[s] = n.apost[s] + 1.0f;
+                    const float ap = __ldg(&n.rule_a[rule * 2 + 0]);
+                    n.w[s] = clamp_w(n.w[s] + ap * n.apre[s], n.wmax[s]);
+                }
+            }
+        }
+    }
+    if (active) {
+        n.v[j] = r.v;
+        n.u[j] = r.u;
+        n.gexc[j] = r.gexc;
+        n.ginh[j] = r.ginh;
+        n.last[j] = r.last;
+    }
+    // warp-aggregated delivered-event count
+    for (int o = 16; o > 0; o >>= 1) delivered += __shfl_down_sync(0xffffffffu, delivered, o);
+    if (lane == 0 && delivered) atomicAdd(n.n_events, delivered);
+}
+
+// Propagate the spikes of the last B steps: one warp per spike, lanes over its
+// out-synapses; also appends the spikes to the run's raster in step order and
+// advances the device clock.  The last CTA to finish publishes the cursor.
+__global__ void __launch_bounds__(256) k_propagate(NetDev n, int B) {
+    __shared__ int pre[kMaxBlockSteps + 1];
+    const int T0 = *n.tnow;
+    const int run_t0 = *n.run_t0;
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int b = 0; b < B; ++b) {
+            pre[b] = s;
+            s += n.blk_cnt[b];
+        }
+        pre[B] = s;
+    }
+    __syncthreads();
+    const int total = pre[B];
+    const long long cur = *n.cursor;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int g = gw; g < total; g += nwarps) {
+        int b = 0;
+        while (b + 1 < B && pre[b + 1] <= g) ++b;
+        const int src = n.blk_spk[(size_t)b * n.N + (g - pre[b])];
+        const unsigned int t = (unsigned int)(T0 + b);
+        if (lane == 0) {
+            if (cur + g < n.out_cap) n.out_ids[cur + g] = src;
+            else atomicOr(n.err, kErrOverflow);
+        }
+        const int q0 = n.out_ptr[src], q1 = n.out_ptr[src + 1];
+        for (int q = q0 + lane; q < q1; q += 32) {
+            const unsigned int bit = n.out_bit[q];
+            const unsigned int slot = (t + n.out_delay[q]) % (unsigned int)n.D;
+            atomicOr(&n.mask[(size_t)slot * n.Wt + (bit >> 5)], 1u << (bit & 31u));
+        }
+    }
+    if (blockIdx.x == 0 && (int)threadIdx.x < B) n.out_cnt[T0 - run_t0 + threadIdx.x] = n.blk_cnt[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int prev = atomicAdd(n.done, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            *n.cursor = cur + total;
+            for (int b = 0; b < B; ++b) n.blk_cnt[b] = 0;
+            *n.tnow = T0 + B;
+            *n.done = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) return cudaSuccess;
+        return cudaMalloc(&p, count * sizeof(T));
+    }
+    cudaError_t upload(const std::vector<T> &h) {
+        cudaError_t e = alloc(h.size());
+        if (e != cudaSuccess || h.empty()) return e;
+        return cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    }
+    cudaError_t zero() { return n ? cudaMemset(p, 0, n * sizeof(T)) : cudaSuccess; }
+};
+
+} // namespace
+
+struct nbg_engine {
+    int device = 0;
+    int N = 0;
+    int64_t S = 0;
+    int D = 1, Wt = 0, dmin = 1, dmax = 1, B = 1;
+    int threads = 256;
+    int n_rules = 0;
+    float dt = 1.0f;
+    int semantics = 0;
+    unsigned long long seed = 0;
+    bool use_graph = true;
+    int64_t spike_capacity = 0;
+    int64_t ev_cap = 0;
+    // host copies
+    std::vector<LayerDev> layers;
+    std::vector<int> csc_ptr;
+    std::vector<int64_t> csc_orig; // CSC position -> original connection index
+    std::vector<int64_t> orig_pos; // original connection index -> CSC position
+    std::vector<nbg_stdp_desc> rules;
+    std::vector<float> init_v, init_u, init_iext;
+    std::vector<float> init_w;
+    // device buffers
+    DevBuf<unsigned short> pop;
+    DevBuf<unsigned char> meta;
+    DevBuf<LayerDev> d_layers;
+    DevBuf<float> v, u, gexc, ginh, iext, w, wmax, apre, apost, dtab, rule_a, trace, ev_w;
+    DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, blk_spk, blk_cnt, out_ids, out_cnt, err, tnow, run_t0,
+        trace_slot, ev_t, ev_pos;
+    DevBuf<unsigned int> mask, out_bit, done;
+    DevBuf<unsigned short> out_delay;
+    DevBuf<long long> cursor;
+    DevBuf<unsigned long long> ev_cursor, n_events;
+    int dtab_len = 0;
+    bool dtab_complete = false; // table reached exact zero: longer gaps decay to 0
+    // time / recording
+    int next_t = 0;
+    bool ran = false;
+    std::vector<int32_t> spk_t, spk_id;
+    std::vector<int32_t> trace_ids;
+    std::vector<float> trace_rows;
+    int64_t trace_nrows = 0;
+    struct CurrentEvent {
+        int t, id;
+        float value;
+    };
+    std::vector<CurrentEvent> currents; // pending, sorted by time
+    std::vector<int32_t> log_t;
+    std::vector<int64_t> log_conn;
+    std::vector<float> log_w;
+    // launch resources
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_blocks = 0, graph_B = 0;
+    NetDev graph_nd{}; // kernel arguments baked into the graph
+    int prop_grid = 0;
+    double last_ms = 0.0, last_upd_ms = 0.0, last_prop_ms = 0.0;
+    int64_t last_launches = 0;
+    bool kernel_timing = false;
+    std::vector<cudaEvent_t> tev; // 3 per block of one graph / launch batch
+    int tev_used = 0;             // blocks bracketed since the last harvest
+
+    NetDev dev() {
+        NetDev n{};
+        n.N = N;
+        n.D = D;
+        n.Wt = Wt;
+        n.n_layers = (int)layers.size();
+        n.semantics = semantics;
+        n.dt = dt;
+        n.seed = seed;
+        n.pop = pop.p;
+        n.layers = d_layers.p;
+        n.v = v.p;
+        n.u = u.p;
+        n.gexc = gexc.p;
+        n.ginh = ginh.p;
+        n.iext = iext.p;
+        n.last = last.p;
+        n.csc_ptr = csc_ptr_d.p;
+        n.woff = woff.p;
+        n.w = w.p;
+        n.wmax = wmax.p;
+        n.meta = meta.p;
+        n.apre = apre.p;
+        n.apost = apost.p;
+        n.slast = slast.p;
+        n.dtab = dtab.p;
+        n.dtab_len = dtab_len;
+        n.rule_a = rule_a.p;
+        n.mask = mask.p;
+        n.out_ptr = out_ptr.p;
+        n.out_bit = out_bit.p;
+        n.out_delay = out_delay.p;
+        n.blk_spk = blk_spk.p;
+        n.blk_cnt = blk_cnt.p;
+        n.out_ids = out_ids.p;
+        n.out_cnt = out_cnt.p;
+        n.cursor = cursor.p;
+        n.out_cap = (long long)out_ids.n;
+        n.err = err.p;
+        n.tnow = tnow.p;
+        n.run_t0 = run_t0.p;
+        n.done = done.p;
+        n.trace_slot = trace_ids.empty() ? nullptr : trace_slot.p;
+        n.trace = trace.p;
+        n.ntrace = (int)trace_ids.size();
+        n.ev_t = ev_cap > 0 ? ev_t.p : nullptr;
+        n.ev_pos = ev_pos.p;
+        n.ev_w = ev_w.p;
+        n.ev_cursor = ev_cursor.p;
+        n.ev_cap = ev_cap;
+        n.n_events = n_events.p;
+        return n;
+    }
+};
+
+namespace {
+
+// Host decay table: table[k] = expf(-((float)k * dt) * inv_tau), the exact
+// float expression of STDP_State::SetUpdate evaluated with the host libm.
+nbg_status ensure_decay_table(nbg_engine *e, int64_t needed) {
+    if (e->n_rules == 0) return NBG_OK;
+    if (e->dtab_complete || e->dtab_len >= needed) return NBG_OK;
+    int64_t len = std::max<int64_t>(needed, 4096);
+    len = std::min<int64_t>(len, (int64_t)1 << 24);
+    std::vector<float> tab((size_t)e->n_rules * 2 * len);
+    bool complete = true;
+    for (int r = 0; r < e->n_rules; ++r) {
+        const float inv_p = (float)(1.0 / (double)e->rules[r].ltp_tau);
+        const float inv_m = (float)(1.0 / (double)e->rules[r].ltd_tau);
+        bool zp = false, zm = false;
+        for (int64_t k = 0; k < len; ++k) {
+            const float dtime = (float)k * e->dt;
+            const float vp = std::exp(-dtime * inv_p);
+            const float vm = std::exp(-dtime * inv_m);
+            tab[(size_t)(r * 2 + 0) * len + k] = vp;
+            tab[(size_t)(r * 2 + 1) * len + k] = vm;
+            if (k == len - 1) {
+                zp = vp == 0.0f;
+                zm = vm == 0.0f;
+            }
+        }
+        complete = complete && zp && zm;
+    }
+    if (!complete && needed > len) return fail(NBG_ERR_UNSUPPORTED, "STDP decay table would exceed 2^24 entries");
+    NBG_CUDA(e->dtab.upload(tab));
+    e->dtab_len = (int)len;
+    e->dtab_complete = complete;
+    return NBG_OK;
+}
+
+nbg_status upload_layers(nbg_engine *e) {
+    NBG_CUDA(e->d_layers.alloc(e->layers.size()));
+    NBG_CUDA(cudaMemcpy(e->d_layers.p, e->layers.data(), e->layers.size() * sizeof(LayerDev),
+                        cudaMemcpyHostToDevice));
+    return NBG_OK;
+}
+
+nbg_status reset_state(nbg_engine *e) {
+    NBG_CUDA(cudaMemcpy(e->v.p, e->init_v.data(), e->N * sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(cudaMemcpy(e->u.p, e->init_u.data(), e->N * sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(cudaMemcpy(e->iext.p, e->init_iext.data(), e->N * sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(e->gexc.zero());
+    NBG_CUDA(e->ginh.zero());
+    std::vector<int> last0((size_t)e->N, 10000);
+    NBG_CUDA(cudaMemcpy(e->last.p, last0.data(), e->N * sizeof(int), cudaMemcpyHostToDevice));
+    if (e->S > 0) {
+        NBG_CUDA(cudaMemcpy(e->w.p, e->init_w.data(), e->S * sizeof(float), cudaMemcpyHostToDevice));
+        NBG_CUDA(e->apre.zero());
+        NBG_CUDA(e->apost.zero());
+        NBG_CUDA(e->slast.zero());
+    }
+    NBG_CUDA(e->mask.zero());
+    NBG_CUDA(e->blk_cnt.zero());
+    NBG_CUDA(e->err.zero());
+    NBG_CUDA(e->tnow.zero());
+    NBG_CUDA(e->done.zero());
+    NBG_CUDA(e->cursor.zero());
+    NBG_CUDA(e->ev_cursor.zero());
+    NBG_CUDA(e->n_events.zero());
+    e->next_t = 0;
+    e->ran = false;
+    e->spk_t.clear();
+    e->spk_id.clear();
+    e->trace_rows.clear();
+    e->trace_nrows = 0;
+    e->log_t.clear();
+    e->log_conn.clear();
+    e->log_w.clear();
+    e->currents.clear();
+    return NBG_OK;
+}
+
+constexpr int kGraphBlocks = 64;
+
+// Launch one block of B steps.  With kernel timing, `slot` selects the event
+// triple bracketing the two kernels.
+void launch_block(nbg_engine *e, const NetDev &nd, int B, int slot) {
+    const int grid = (e->N + e->threads - 1) / e->threads;
+    if (e->kernel_timing) cudaEventRecord(e->tev[3 * slot + 0], e->stream);
+    k_update<<<grid, e->threads, 0, e->stream>>>(nd, B);
+    if (e->kernel_timing) cudaEventRecord(e->tev[3 * slot + 1], e->stream);
+    k_propagate<<<e->prop_grid, 256, 0, e->stream>>>(nd, B);
+    if (e->kernel_timing) cudaEventRecord(e->tev[3 * slot + 2], e->stream);
+}
+
+// Sum the bracketed kernel durations of `blocks` event triples.
+nbg_status harvest_timing(nbg_engine *e, int blocks) {
+    if (!e->kernel_timing || blocks == 0) return NBG_OK;
+    NBG_CUDA(cudaEventSynchronize(e->tev[3 * (blocks - 1) + 2]));
+    for (int k = 0; k < blocks; ++k) {
+        float a = 0.0f, b = 0.0f;
+        NBG_CUDA(cudaEventElapsedTime(&a, e->tev[3 * k + 0], e->tev[3 * k + 1]));
+        NBG_CUDA(cudaEventElapsedTime(&b, e->tev[3 * k + 1], e->tev[3 * k + 2]));
+        e->last_upd_ms += a;
+        e->last_prop_ms += b;
+    }
+    return NBG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *nbg_last_error(void) { return g_err.c_str(); }
+const char *nbg_version(void) { return "nbg 0.1 (sm_103a)"; }
+
+void nbg_default_options(nbg_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->device = 0;
+    o->block_steps = 0;
+    o->threads_per_block = 256;
+    o->spike_capacity = 0;
+    o->use_graph = 1;
+    o->event_log_capacity = 0;
+    o->kernel_timing = 0;
+}
+
+nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engine **out) {
+    if (!d || !out) return fail(NBG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    nbg_options opt;
+    nbg_default_options(&opt);
+    if (opt_in) opt = *opt_in;
+    if (d->n_layers <= 0 || d->n_layers > 65535 || !d->layers)
+        return fail(NBG_ERR_INVALID, "need 1..65535 layers");
+    if (!(d->dt_ms > 0.0f)) return fail(NBG_ERR_INVALID, "timestep must be positive");
+    if (d->semantics != NBG_SEM_LEGACY_CPU && d->semantics != NBG_SEM_DENSE)
+        return fail(NBG_ERR_INVALID, "unknown semantics %d", d->semantics);
+    if (d->n_conn < 0 || d->n_conn > 0x7FFFFFFFll) return fail(NBG_ERR_INVALID, "connection count out of range");
+    if (d->n_conn > 0 && (!d->source || !d->target || !d->type || !d->weight || !d->max_weight || !d->delay ||
+                          !d->rule))
+        return fail(NBG_ERR_INVALID, "connection arrays must be non-null");
+    if (d->n_rules < 0 || d->n_rules > 126 || (d->n_rules > 0 && !d->rules))
+        return fail(NBG_ERR_INVALID, "need 0..126 learning rules");
+    if (opt.threads_per_block <= 0) opt.threads_per_block = 256;
+    if (opt.threads_per_block % 32 || opt.threads_per_block > 256)
+        return fail(NBG_ERR_INVALID, "threads_per_block must be a multiple of 32 and <= 256");
+
+    int64_t total = 0;
+    for (int l = 0; l < d->n_layers; ++l) {
+        const nbg_layer_desc &ld = d->layers[l];
+        if (ld.model < 0 || ld.model > 3) return fail(NBG_ERR_INVALID, "layer %d: unknown model %d", l, ld.model);
+        if (ld.count <= 0) return fail(NBG_ERR_INVALID, "layer %d: count must be positive", l);
+        total += ld.count;
+    }
+    if (total > (1 << 30)) return fail(NBG_ERR_INVALID, "too many neurons");
+    for (int r = 0; r < d->n_rules; ++r)
+        if (!(d->rules[r].ltp_tau > 0.0f) || !(d->rules[r].ltd_tau > 0.0f))
+            return fail(NBG_ERR_INVALID, "rule %d: time constants must be positive", r);
+
+    auto *e = new nbg_engine();
+    e->device = opt.device;
+    e->N = (int)total;
+    e->S = d->n_conn;
+    e->dt = d->dt_ms;
+    e->semantics = d->semantics;
+    e->seed = d->seed;
+    e->threads = opt.threads_per_block;
+    e->use_graph = opt.use_graph != 0;
+    e->ev_cap = opt.event_log_capacity;
+    e->kernel_timing = opt.kernel_timing != 0;
+    e->n_rules = d->n_rules;
+    e->rules.assign(d->rules, d->rules + d->n_rules);
+    auto bail = [&](nbg_status s) {
+        delete e;
+        return s;
+    };
+    // ---- layers
+    std::vector<unsigned short> pop((size_t)e->N);
+    e->layers.resize(d->n_layers);
+    e->init_v.assign(e->N, 0.0f);
+    e->init_u.assign(e->N, 0.0f);
+    e->init_iext.assign(e->N, 0.0f);
+    int start = 0;
+    for (int l = 0; l < d->n_layers; ++l) {
+        const nbg_layer_desc &ld = d->layers[l];
+        LayerDev L{};
+        L.model = ld.model;
+        L.start = start;
+        L.count = ld.count;
+        std::memcpy(L.f, ld.f, sizeof(L.f));
+        std::memcpy(L.ip, ld.ip, sizeof(L.ip));
+        if (ld.model == NBG_MODEL_IZH_COND) {
+            const float inv_a = ld.f[8] != 0.0f ? 1.0f / ld.f[8] : 0.0f;
+            const float inv_g = ld.f[10] != 0.0f ? 1.0f / ld.f[10] : 0.0f;
+            L.decay_exc = std::exp(-d->dt_ms * inv_a);
+            L.decay_inh = std::exp(-d->dt_ms * inv_g);
+        }
+        if (ld.model == NBG_MODEL_LIF_VJ) {
+            if (!(ld.f[1] != 0.0f)) return bail(fail(NBG_ERR_INVALID, "layer %d: tau must be non-zero", l));
+            L.alpha = d->dt_ms / ld.f[1];
+        }
+        for (int i = start; i < start + ld.count; ++i) {
+            pop[i] = (unsigned short)l;
+            switch (ld.model) {
+            case NBG_MODEL_LIF_VJ:
+                e->init_v[i] = d->semantics == NBG_SEM_DENSE ? ld.f[0] : ld.f[4] + ld.f[5];
+                e->init_iext[i] = ld.f[6];
+                break;
+            case NBG_MODEL_IZH_COND:
+                e->init_v[i] = ld.f[4];
+                e->init_u[i] = ld.f[1] * ld.f[4];
+                e->init_iext[i] = ld.f[11];
+                break;
+            case NBG_MODEL_IZH_RK4:
+                e->init_v[i] = ld.f[4];
+                e->init_u[i] = ld.f[1] * ld.f[4];
+                e->init_iext[i] = ld.f[7];
+                break;
+            default:
+                e->init_iext[i] = ld.f[2];
+                break;
+            }
+        }
+        e->layers[l] = L;
+        start += ld.count;
+    }
+
+    // ---- validate connections, CSC order by (target, source, delay, index)
+    const int64_t S = d->n_conn;
+    e->dmin = 0x7FFFFFFF;
+    e->dmax = 1;
+    std::vector<int> indeg((size_t)e->N + 1, 0);
+    for (int64_t s = 0; s < S; ++s) {
+        const int a = d->source[s], b = d->target[s];
+        if (a < 0 || a >= e->N || b < 0 || b >= e->N)
+            return bail(fail(NBG_ERR_INVALID, "connection %lld: neuron id out of range", (long long)s));
+        if (d->delay[s] < 1 || d->delay[s] > 65535)
+            return bail(fail(NBG_ERR_INVALID, "connection %lld: delay must be in 1..65535 steps", (long long)s));
+        if (d->type[s] != 0 && d->type[s] != 1)
+            return bail(fail(NBG_ERR_UNSUPPORTED, "connection %lld: synapse type %d not supported (0 exc, 1 inh)",
+                             (long long)s, d->type[s]));
+        if (d->rule[s] < -1 || d->rule[s] >= d->n_rules)
+            return bail(fail(NBG_ERR_INVALID, "connection %lld: learning rule %d out of range", (long long)s,
+                             d->rule[s]));
+        if (!std::isfinite(d->weight[s]) || !std::isfinite(d->max_weight[s]))
+            return bail(fail(NBG_ERR_INVALID, "connection %lld: weight must be finite", (long long)s));
+        e->dmin = std::min(e->dmin, d->delay[s]);
+        e->dmax = std::max(e->dmax, d->delay[s]);
+        indeg[b + 1]++;
+        if (d->type[s] == 0) e->layers[pop[b]].has_exc = 1;
+        else e->layers[pop[b]].has_inh = 1;
+    }
+    if (S == 0) e->dmin = kMaxBlockSteps;
+    std::vector<int> &cptr = e->csc_ptr;
+    cptr.assign((size_t)e->N + 1, 0);
+    for (int i = 0; i < e->N; ++i) cptr[i + 1] = cptr[i] + indeg[i + 1];
+    e->csc_orig.assign((size_t)S, 0);
+    {
+        std::vector<int> fill(cptr.begin(), cptr.end() - 1);
+        for (int64_t s = 0; s < S; ++s) e->csc_orig[fill[d->target[s]]++] = s; // stable by index
+        for (int j = 0; j < e->N; ++j) {
+            auto first = e->csc_orig.begin() + cptr[j], last_it = e->csc_orig.begin() + cptr[j + 1];
+            std::sort(first, last_it, [&](int64_t x, int64_t y) {
+                if (d->source[x] != d->source[y]) return d->source[x] < d->source[y];
+                if (d->delay[x] != d->delay[y]) return d->delay[x] < d->delay[y];
+                return x < y;
+            });
+        }
+    }
+    e->orig_pos.assign((size_t)S, 0);
+    for (int64_t p = 0; p < S; ++p) e->orig_pos[e->csc_orig[p]] = p;
+
+    // ---- mask word offsets and per-synapse arrays
+    std::vector<int> woff((size_t)e->N + 1, 0);
+    for (int j = 0; j < e->N; ++j) woff[j + 1] = woff[j] + (cptr[j + 1] - cptr[j] + 31) / 32;
+    e->Wt = std::max(woff[e->N], 1);
+    e->D = e->dmax + 1;
+    std::vector<float> w((size_t)S), wmax((size_t)S);
+    std::vector<unsigned char> meta((size_t)S);
+    std::vector<int> src_of((size_t)S);
+    for (int64_t p = 0; p < S; ++p) {
+        const int64_t s = e->csc_orig[p];
+        w[p] = d->weight[s];
+        wmax[p] = d->max_weight[s];
+        meta[p] = (unsigned char)((d->type[s] & 1) | ((d->rule[s] + 1) << 1));
+        src_of[p] = d->source[s];
+    }
+    e->init_w = w;
+
+    // ---- CSR by source over (mask bit, delay)
+    std::vector<int> optr((size_t)e->N + 1, 0);
+    for (int64_t p = 0; p < S; ++p) optr[src_of[p] + 1]++;
+    for (int i = 0; i < e->N; ++i) optr[i + 1] += optr[i];
+    std::vector<unsigned int> obit((size_t)S);
+    std::vector<unsigned short> odelay((size_t)S);
+    {
+        std::vector<int> fill(optr.begin(), optr.end() - 1);
+        for (int j = 0; j < e->N; ++j)
+            for (int p = cptr[j]; p < cptr[j + 1]; ++p) {
+                const int q = fill[src_of[p]]++;
+                obit[q] = (unsigned int)woff[j] * 32u + (unsigned int)(p - cptr[j]);
+                odelay[q] = (unsigned short)d->delay[e->csc_orig[p]];
+            }
+    }
+    if ((uint64_t)e->Wt * 32ull > 0xFFFFFFFFull) return bail(fail(NBG_ERR_UNSUPPORTED, "too many synapses"));
+
+    int B = opt.block_steps > 0 ? std::min(opt.block_steps, e->dmin) : e->dmin;
+    e->B = std::max(1, std::min(B, kMaxBlockSteps));
+
+    // ---- device allocation
+    if (cudaSetDevice(e->device) != cudaSuccess)
+        return bail(fail(NBG_ERR_CUDA, "cudaSetDevice(%d) failed: no usable CUDA device", opt.device));
+    nbg_status st = NBG_OK;
+    auto chk = [&](cudaError_t ce, const char *what) {
+        if (ce != cudaSuccess && st == NBG_OK)
+            st = fail(ce == cudaErrorMemoryAllocation ? NBG_ERR_OOM : NBG_ERR_CUDA, "%s: %s", what,
+                      cudaGetErrorString(ce));
+    };
+    chk(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
+    chk(cudaEventCreate(&e->ev0), "event");
+    chk(cudaEventCreate(&e->ev1), "event");
+    if (e->kernel_timing) {
+        e->tev.resize(3 * kGraphBlocks, nullptr);
+        for (auto &ev : e->tev) chk(cudaEventCreate(&ev), "timing event");
+    }
+    chk(e->pop.upload(pop), "pop");
+    chk(e->meta.upload(meta), "meta");
+    const size_t N = (size_t)e->N;
+    chk(e->v.alloc(N), "v");
+    chk(e->u.alloc(N), "u");
+    chk(e->gexc.alloc(N), "gexc");
+    chk(e->ginh.alloc(N), "ginh");
+    chk(e->iext.alloc(N), "iext");
+    chk(e->last.alloc(N), "last");
+    chk(e->csc_ptr_d.upload(cptr), "csc_ptr");
+    chk(e->woff.upload(woff), "woff");
+    chk(e->w.alloc((size_t)S), "w");
+    chk(e->wmax.upload(wmax), "wmax");
+    chk(e->apre.alloc((size_t)S), "apre");
+    chk(e->apost.alloc((size_t)S), "apost");
+    chk(e->slast.alloc((size_t)S), "slast");
+    chk(e->mask.alloc((size_t)e->D * e->Wt), "mask ring");
+    chk(e->out_ptr.upload(optr), "out_ptr");
+    chk(e->out_bit.upload(obit), "out_bit");
+    chk(e->out_delay.upload(odelay), "out_delay");
+    chk(e->blk_spk.alloc((size_t)kMaxBlockSteps * N), "block spike lists");
+    chk(e->blk_cnt.alloc(kMaxBlockSteps), "block counts");
+    chk(e->err.alloc(1), "err");
+    chk(e->tnow.alloc(1), "tnow");
+    chk(e->run_t0.alloc(1), "run_t0");
+    chk(e->done.alloc(1), "done");
+    chk(e->cursor.alloc(1), "cursor");
+    chk(e->ev_cursor.alloc(1), "ev_cursor");
+    chk(e->n_events.alloc(1), "n_events");
+    if (e->ev_cap > 0) {
+        chk(e->ev_t.alloc((size_t)e->ev_cap), "event log");
+        chk(e->ev_pos.alloc((size_t)e->ev_cap), "event log");
+        chk(e->ev_w.alloc((size_t)e->ev_cap), "event log");
+    }
+    {
+        std::vector<float> ra((size_t)std::max(1, e->n_rules) * 2, 0.0f);
+        for (int r = 0; r < e->n_rules; ++r) {
+            ra[r * 2 + 0] = e->rules[r].max_ltp;
+            ra[r * 2 + 1] = e->rules[r].max_ltd;
+        }
+        chk(e->rule_a.upload(ra), "rule params");
+    }
+    if (st != NBG_OK) return bail(st);
+    st = upload_layers(e);
+    if (st == NBG_OK) st = ensure_decay_table(e, 4096);
+    if (st == NBG_OK) st = reset_state(e);
+    if (st != NBG_OK) return bail(st);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
+    e->prop_grid = std::max(1, sms) * 4;
+    e->spike_capacity = opt.spike_capacity;
+    *out = e;
+    return NBG_OK;
+}
+
+nbg_status nbg_destroy(nbg_engine *e) {
+    if (!e) return NBG_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    for (auto ev : e->tev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return NBG_OK;
+}
+
+nbg_status nbg_reset(nbg_engine *e) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    return reset_state(e);
+}
+
+nbg_status nbg_run(nbg_engine *e, int steps) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (steps <= 0) return fail(NBG_ERR_INVALID, "Simulation.run steps must be positive");
+    NBG_CUDA(cudaSetDevice(e->device));
+    const int count = e->ran ? steps : steps + 1;
+    if ((int64_t)e->next_t + count > 0x7FFFFFF0ll) return fail(NBG_ERR_INVALID, "simulation time overflow");
+    nbg_status st = ensure_decay_table(e, (int64_t)e->next_t + count + 1);
+    if (st != NBG_OK) return st;
+    // raster capacity for this call
+    int64_t cap = e->spike_capacity > 0 ? e->spike_capacity
+                                        : std::min<int64_t>((int64_t)e->N * count, (int64_t)1 << 26);
+    cap = std::max<int64_t>(cap, 1);
+    if ((int64_t)e->out_ids.n < cap) NBG_CUDA(e->out_ids.alloc((size_t)cap));
+    if ((int64_t)e->out_cnt.n < count) NBG_CUDA(e->out_cnt.alloc((size_t)count));
+    const int ntr = (int)e->trace_ids.size();
+    if (ntr > 0 && (int64_t)e->trace.n < (int64_t)count * ntr) NBG_CUDA(e->trace.alloc((size_t)count * ntr));
+    const int t0 = e->next_t;
+    NBG_CUDA(cudaMemcpyAsync(e->run_t0.p, &t0, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+    NBG_CUDA(cudaMemsetAsync(e->cursor.p, 0, sizeof(long long), e->stream));
+    NBG_CUDA(cudaMemsetAsync(e->err.p, 0, sizeof(int), e->stream));
+    const NetDev nd = e->dev();
+
+    e->last_upd_ms = 0.0;
+    e->last_prop_ms = 0.0;
+    NBG_CUDA(cudaEventRecord(e->ev0, e->stream));
+    const int B = e->B;
+    int64_t launches = 0;
+    // pending current events inside this call split it into segments
+    std::vector<nbg_engine::CurrentEvent> due;
+    {
+        std::vector<nbg_engine::CurrentEvent> later;
+        for (const auto &c : e->currents) {
+            if (c.t < t0) continue; // already past: dropped
+            (c.t < t0 + count ? due : later).push_back(c);
+        }
+        e->currents.swap(later);
+    }
+    int t = t0;
+    size_t ci = 0;
+    const int t_end = t0 + count;
+    while (t < t_end) {
+        while (ci < due.size() && due[ci].t == t) {
+            NBG_CUDA(cudaMemcpyAsync(e->iext.p + due[ci].id, &due[ci].value, sizeof(float), cudaMemcpyHostToDevice,
+                                     e->stream));
+            NBG_CUDA(cudaStreamSynchronize(e->stream)); // the host value is a stack copy
+            ++ci;
+        }
+        const int seg_end = ci < due.size() ? due[ci].t : t_end;
+        const int seg = seg_end - t;
+        const int nfull = seg / B, tail = seg % B;
+        int done_blocks = 0;
+        if (e->use_graph && nfull >= 8) {
+            const int G = std::min(nfull, kGraphBlocks);
+            if (!e->graph || e->graph_blocks != G || e->graph_B != B ||
+                std::memcmp(&e->graph_nd, &nd, sizeof(NetDev)) != 0) {
+                if (e->graph) {
+                    cudaGraphExecDestroy(e->graph);
+                    e->graph = nullptr;
+                }
+                cudaGraph_t g;
+                NBG_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < G; ++k) launch_block(e, nd, B, k);
+                NBG_CUDA(cudaStreamEndCapture(e->stream, &g));
+                cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+                cudaGraphDestroy(g);
+                if (ie != cudaSuccess) return fail(NBG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+                e->graph_blocks = G;
+                e->graph_B = B;
+                e->graph_nd = nd;
+            }
+            const int reps = nfull / G;
+            for (int k = 0; k < reps; ++k) {
+                NBG_CUDA(cudaGraphLaunch(e->graph, e->stream));
+                nbg_status hs = harvest_timing(e, G); // event triples are reused by the next replay
+                if (hs != NBG_OK) return hs;
+            }
+            done_blocks = reps * G;
+            launches += (int64_t)reps * G * 2;
+        }
+        int slot = 0;
+        for (int k = done_blocks; k < nfull + (tail ? 1 : 0); ++k) {
+            launch_block(e, nd, k < nfull ? B : tail, slot++);
+            launches += 2;
+            if (slot == kGraphBlocks) {
+                nbg_status hs = harvest_timing(e, slot);
+                if (hs != NBG_OK) return hs;
+                slot = 0;
+            }
+        }
+        {
+            nbg_status hs = harvest_timing(e, slot);
+            if (hs != NBG_OK) return hs;
+        }
+        t = seg_end;
+    }
+    NBG_CUDA(cudaGetLastError());
+    NBG_CUDA(cudaEventRecord(e->ev1, e->stream));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+    e->last_ms = ms;
+    e->last_launches = launches;
+
+    int errv = 0;
+    long long nspk = 0;
+    NBG_CUDA(cudaMemcpy(&errv, e->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    NBG_CUDA(cudaMemcpy(&nspk, e->cursor.p, sizeof(long long), cudaMemcpyDeviceToHost));
+    e->next_t += count;
+    e->ran = true;
+    if (errv & kErrEventLog) return fail(NBG_ERR_OVERFLOW, "delivered-event log capacity exceeded");
+    if (errv & kErrOverflow)
+        return fail(NBG_ERR_OVERFLOW, "spike raster capacity (%lld) exceeded in this run call", (long long)cap);
+    // raster: per-step counts and ids, sorted by id within a step
+    std::vector<int> cnt((size_t)count);
+    NBG_CUDA(cudaMemcpy(cnt.data(), e->out_cnt.p, count * sizeof(int), cudaMemcpyDeviceToHost));
+    const size_t base = e->spk_id.size();
+    e->spk_id.resize(base + (size_t)nspk);
+    e->spk_t.resize(base + (size_t)nspk);
+    if (nspk > 0)
+        NBG_CUDA(cudaMemcpy(e->spk_id.data() + base, e->out_ids.p, nspk * sizeof(int), cudaMemcpyDeviceToHost));
+    size_t off = base;
+    for (int k = 0; k < count; ++k) {
+        std::sort(e->spk_id.begin() + off, e->spk_id.begin() + off + cnt[k]);
+        std::fill(e->spk_t.begin() + off, e->spk_t.begin() + off + cnt[k], t0 + k);
+        off += cnt[k];
+    }
+    if (ntr > 0) {
+        const size_t rb = e->trace_rows.size();
+        e->trace_rows.resize(rb + (size_t)count * ntr);
+        NBG_CUDA(cudaMemcpy(e->trace_rows.data() + rb, e->trace.p, (size_t)count * ntr * sizeof(float),
+                            cudaMemcpyDeviceToHost));
+        e->trace_nrows += count;
+    }
+    if (e->ev_cap > 0) {
+        unsigned long long nev = 0;
+        NBG_CUDA(cudaMemcpy(&nev, e->ev_cursor.p, sizeof(nev), cudaMemcpyDeviceToHost));
+        std::vector<int> et((size_t)nev), ep((size_t)nev);
+        std::vector<float> ew((size_t)nev);
+        if (nev) {
+            NBG_CUDA(cudaMemcpy(et.data(), e->ev_t.p, nev * sizeof(int), cudaMemcpyDeviceToHost));
+            NBG_CUDA(cudaMemcpy(ep.data(), e->ev_pos.p, nev * sizeof(int), cudaMemcpyDeviceToHost));
+            NBG_CUDA(cudaMemcpy(ew.data(), e->ev_w.p, nev * sizeof(float), cudaMemcpyDeviceToHost));
+        }
+        for (size_t k = 0; k < nev; ++k) {
+            e->log_t.push_back(et[k]);
+            e->log_conn.push_back(e->csc_orig[ep[k]]);
+            e->log_w.push_back(ew[k]);
+        }
+        NBG_CUDA(cudaMemset(e->ev_cursor.p, 0, sizeof(unsigned long long)));
+    }
+    return NBG_OK;
+}
+
+nbg_status nbg_next_time(const nbg_engine *e, int *t) {
+    if (!e || !t) return fail(NBG_ERR_INVALID, "null argument");
+    *t = e->next_t;
+    return NBG_OK;
+}
+nbg_status nbg_num_neurons(const nbg_engine *e, int *n) {
+    if (!e || !n) return fail(NBG_ERR_INVALID, "null argument");
+    *n = e->N;
+    return NBG_OK;
+}
+nbg_status nbg_num_synapses(const nbg_engine *e, int64_t *s) {
+    if (!e || !s) return fail(NBG_ERR_INVALID, "null argument");
+    *s = e->S;
+    return NBG_OK;
+}
+nbg_status nbg_block_steps(const nbg_engine *e, int *b) {
+    if (!e || !b) return fail(NBG_ERR_INVALID, "null argument");
+    *b = e->B;
+    return NBG_OK;
+}
+
+nbg_status nbg_get_state(nbg_engine *e, int field, float *out) {
+    if (!e || !out) return fail(NBG_ERR_INVALID, "null argument");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    const size_t bytes = (size_t)e->N * sizeof(float);
+    switch (field) {
+    case NBG_FIELD_V: NBG_CUDA(cudaMemcpy(out, e->v.p, bytes, cudaMemcpyDeviceToHost)); break;
+    case NBG_FIELD_U: NBG_CUDA(cudaMemcpy(out, e->u.p, bytes, cudaMemcpyDeviceToHost)); break;
+    case NBG_FIELD_G_EXC: NBG_CUDA(cudaMemcpy(out, e->gexc.p, bytes, cudaMemcpyDeviceToHost)); break;
+    case NBG_FIELD_G_INH: NBG_CUDA(cudaMemcpy(out, e->ginh.p, bytes, cudaMemcpyDeviceToHost)); break;
+    case NBG_FIELD_I_EXT: NBG_CUDA(cudaMemcpy(out, e->iext.p, bytes, cudaMemcpyDeviceToHost)); break;
+    case NBG_FIELD_LAST_SPIKE: {
+        std::vector<int> tmp((size_t)e->N);
+        NBG_CUDA(cudaMemcpy(tmp.data(), e->last.p, (size_t)e->N * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < e->N; ++i) out[i] = (float)tmp[i];
+        break;
+    }
+    default: return fail(NBG_ERR_INVALID, "unknown state field %d", field);
+    }
+    return NBG_OK;
+}
+
+nbg_status nbg_set_state(nbg_engine *e, int field, const float *in) {
+    if (!e || !in) return fail(NBG_ERR_INVALID, "null argument");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    const size_t bytes = (size_t)e->N * sizeof(float);
+    switch (field) {
+    case NBG_FIELD_V: NBG_CUDA(cudaMemcpy(e->v.p, in, bytes, cudaMemcpyHostToDevice)); break;
+    case NBG_FIELD_U: NBG_CUDA(cudaMemcpy(e->u.p, in, bytes, cudaMemcpyHostToDevice)); break;
+    case NBG_FIELD_I_EXT: NBG_CUDA(cudaMemcpy(e->iext.p, in, bytes, cudaMemcpyHostToDevice)); break;
+    default: return fail(NBG_ERR_INVALID, "state field %d is not writable", field);
+    }
+    return NBG_OK;
+}
+
+nbg_status nbg_num_spikes(nbg_engine *e, int64_t *n) {
+    if (!e || !n) return fail(NBG_ERR_INVALID, "null argument");
+    *n = (int64_t)e->spk_id.size();
+    return NBG_OK;
+}
+
+nbg_status nbg_get_spikes(nbg_engine *e, int32_t *times, int32_t *ids, int64_t capacity) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    const int64_t n = (int64_t)e->spk_id.size();
+    if (capacity < n) return fail(NBG_ERR_OVERFLOW, "need capacity %lld", (long long)n);
+    if (n && times) std::memcpy(times, e->spk_t.data(), n * sizeof(int32_t));
+    if (n && ids) std::memcpy(ids, e->spk_id.data(), n * sizeof(int32_t));
+    return NBG_OK;
+}
+
+nbg_status nbg_clear_spikes(nbg_engine *e) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    e->spk_t.clear();
+    e->spk_id.clear();
+    return NBG_OK;
+}
+
+nbg_status nbg_num_events(nbg_engine *e, int64_t *n) {
+    if (!e || !n) return fail(NBG_ERR_INVALID, "null argument");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    unsigned long long v = 0;
+    NBG_CUDA(cudaMemcpy(&v, e->n_events.p, sizeof(v), cudaMemcpyDeviceToHost));
+    *n = (int64_t)v;
+    return NBG_OK;
+}
+
+nbg_status nbg_get_weights(nbg_engine *e, float *w, float *apre, float *apost, int32_t *last) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    const size_t S = (size_t)e->S;
+    if (S == 0) return NBG_OK;
+    std::vector<float> tmp(S);
+    std::vector<int> itmp;
+    float *dst[3] = {w, apre, apost};
+    float *srcs[3] = {e->w.p, e->apre.p, e->apost.p};
+    for (int k = 0; k < 3; ++k) {
+        if (!dst[k]) continue;
+        NBG_CUDA(cudaMemcpy(tmp.data(), srcs[k], S * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < S; ++p) dst[k][e->csc_orig[p]] = tmp[p];
+    }
+    if (last) {
+        itmp.resize(S);
+        NBG_CUDA(cudaMemcpy(itmp.data(), e->slast.p, S * sizeof(int), cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < S; ++p) last[e->csc_orig[p]] = itmp[p];
+    }
+    return NBG_OK;
+}
+
+nbg_status nbg_set_weight(nbg_engine *e, int64_t conn, float w) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (conn < 0 || conn >= e->S) return fail(NBG_ERR_INVALID, "connection index %lld out of range", (long long)conn);
+    if (!std::isfinite(w)) return fail(NBG_ERR_INVALID, "weight must be finite");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    const int64_t p = e->orig_pos[conn];
+    NBG_CUDA(cudaMemcpy(e->w.p + p, &w, sizeof(float), cudaMemcpyHostToDevice));
+    e->init_w[p] = w;
+    return NBG_OK;
+}
+
+nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (id < 0 || id >= e->N) return fail(NBG_ERR_INVALID, "neuron id %d out of range", id);
+    if (t < e->next_t) return fail(NBG_ERR_INVALID, "time %d is in the past (next step %d)", t, e->next_t);
+    if (!std::isfinite(value)) return fail(NBG_ERR_INVALID, "current must be finite");
+    nbg_engine::CurrentEvent c{t, id, value};
+    auto it = std::upper_bound(e->currents.begin(), e->currents.end(), c,
+                               [](const nbg_engine::CurrentEvent &a, const nbg_engine::CurrentEvent &b) {
+                                   return a.t < b.t;
+                               });
+    e->currents.insert(it, c);
+    return NBG_OK;
+}
+
+nbg_status nbg_set_trace(nbg_engine *e, int n, const int32_t *ids) {
+    if (!e || (n > 0 && !ids) || n < 0) return fail(NBG_ERR_INVALID, "bad trace arguments");
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    std::vector<int> slot((size_t)e->N, -1);
+    for (int k = 0; k < n; ++k) {
+        if (ids[k] < 0 || ids[k] >= e->N) return fail(NBG_ERR_INVALID, "trace id %d out of range", ids[k]);
+        if (slot[ids[k]] >= 0) return fail(NBG_ERR_INVALID, "trace id %d listed twice", ids[k]);
+        slot[ids[k]] = k;
+    }
+    NBG_CUDA(e->trace_slot.upload(slot));
+    e->trace_ids.assign(ids, ids + n);
+    e->trace_rows.clear();
+    e->trace_nrows = 0;
+    return NBG_OK;
+}
+
+nbg_status nbg_num_trace_rows(nbg_engine *e, int64_t *rows) {
+    if (!e || !rows) return fail(NBG_ERR_INVALID, "null argument");
+    *rows = e->trace_nrows;
+    return NBG_OK;
+}
+
+nbg_status nbg_get_traces(nbg_engine *e, float *out) {
+    if (!e || !out) return fail(NBG_ERR_INVALID, "null argument");
+    if (!e->trace_rows.empty()) std::memcpy(out, e->trace_rows.data(), e->trace_rows.size() * sizeof(float));
+    return NBG_OK;
+}
+
+nbg_status nbg_num_logged_events(nbg_engine *e, int64_t *n) {
+    if (!e || !n) return fail(NBG_ERR_INVALID, "null argument");
+    *n = (int64_t)e->log_t.size();
+    return NBG_OK;
+}
+
+nbg_status nbg_get_logged_events(nbg_engine *e, int32_t *t, int64_t *conn, float *w) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    const size_t n = e->log_t.size();
+    if (n && t) std::memcpy(t, e->log_t.data(), n * sizeof(int32_t));
+    if (n && conn) std::memcpy(conn, e->log_conn.data(), n * sizeof(int64_t));
+    if (n && w) std::memcpy(w, e->log_w.data(), n * sizeof(float));
+    return NBG_OK;
+}
+
+nbg_status nbg_profile(nbg_engine *e, double *total_ms, double *update_ms, double *propagate_ms,
+                       int64_t *launches) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (total_ms) *total_ms = e->last_ms;
+    if (update_ms) *update_ms = e->last_upd_ms;
+    if (propagate_ms) *propagate_ms = e->last_prop_ms;
+    if (launches) *launches = e->last_launches;
+    return NBG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,187 @@
+"""GPU engine vs the CPU oracle on identical seeded inputs (bit-exact).
+
+Every comparison here is exact: spike rasters, membrane traces, final state,
+weights and STDP traces, and the delivered-event multiset.  The engine is
+built with -fmad=false and the oracle with -ffp-contract=off, and arrivals
+are applied per target in the same canonical (CSC) order, so every float
+operation matches.  Size-independent properties (determinism, composition of
+run calls, invariance to launch shape, instance independence in a batch) are
+checked at larger sizes.
+"""
+import numpy as np
+import pytest
+
+import neuronbridge_gb300 as nb
+from neuronbridge_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(net, cfg, **kw):
+    import oracle
+
+    return oracle.OracleNet(net.to_native().flat(cfg.timestep, **kw))
+
+
+def _raster_equal(a, b):
+    (ta, ia), (tb, ib) = a, b
+    return len(ta) == len(tb) and np.array_equal(ta, tb) and np.array_equal(ia, ib)
+
+
+def _oracle_raster(o):
+    t, i = o.spikes()
+    order = np.lexsort((i, t))
+    return t[order], i[order]
+
+
+def test_plain_lif_10k_steps_bit_exact(oracle_lib):
+    net, cfg = workloads.plain_lif()  # 1000 LIF + 1000 Poisson, 10,000 steps
+    trace_ids = np.arange(0, 1000, 100)
+    sim = nb.Simulation(net, cfg)
+    sim.set_trace(trace_ids)
+    sim.run()
+    o = _oracle(net, cfg)
+    o.set_trace(trace_ids)
+    o.run(cfg.steps)
+    assert sim.next_time == o.next_time == cfg.steps + 1
+    assert _raster_equal(sim.spike_raster(), _oracle_raster(o))
+    assert np.array_equal(sim.traces(), o.traces().astype(np.float32))
+    assert np.array_equal(sim.state_field(0), o.state(0).astype(np.float32))
+    assert np.array_equal(sim.state_field(6), o.state(6).astype(np.float32))
+    assert sim.num_events == o.num_events > 0
+
+
+def test_delivered_event_multiset_bit_exact(oracle_lib):
+    net, cfg = workloads.plain_lif(steps=400)
+    sim = nb.Simulation(net, cfg, event_log_capacity=2_000_000)
+    sim.run(400)
+    o = _oracle(net, cfg)
+    o.set_event_log(True)
+    o.run(400)
+    gt, gc, gw = sim.logged_events()
+    ot, oc, ow = o.events()
+    g = np.lexsort((gc, gt))
+    k = np.lexsort((oc, ot))
+    assert len(gt) == len(ot) > 0
+    assert np.array_equal(gt[g], ot[k]) and np.array_equal(gc[g], oc[k])
+    assert np.array_equal(gw[g], ow[k].astype(np.float32))
+
+
+def test_izhikevich_stdp_small_bit_exact(oracle_lib):
+    net, cfg = workloads.izhikevich_stdp(n=3000, in_degree=100)
+    sim = nb.Simulation(net, cfg, seed=2)
+    sim.set_trace([0, 1, 2999])
+    sim.run(3000)
+    o = _oracle(net, cfg, seed=2)
+    o.set_trace([0, 1, 2999])
+    o.run(3000)
+    assert _raster_equal(sim.spike_raster(), _oracle_raster(o))
+    assert len(sim.spike_raster()[0]) > 0
+    assert np.array_equal(sim.traces(), o.traces().astype(np.float32))
+    for f in (0, 1, 6):
+        assert np.array_equal(sim.state_field(f), o.state(f).astype(np.float32)), f
+    gw = sim.weights()
+    ow, oa, ob, ol = o.weights()
+    assert np.array_equal(gw["weight"], ow.astype(np.float32))
+    assert np.array_equal(gw["apre"], oa.astype(np.float32))
+    assert np.array_equal(gw["apost"], ob.astype(np.float32))
+    assert np.array_equal(gw["last_update"], ol)
+    assert not np.array_equal(gw["weight"], net.to_native().weight)  # STDP moved weights
+
+
+def test_izhikevich_full_size_short_horizon_bit_exact(oracle_lib):
+    net, cfg = workloads.izhikevich_stdp()  # 100k neurons, 10M synapses
+    sim = nb.Simulation(net, cfg, seed=2)
+    sim.run(400)
+    o = _oracle(net, cfg, seed=2)
+    o.run(400)
+    assert _raster_equal(sim.spike_raster(), _oracle_raster(o))
+    assert np.array_equal(sim.state_field(0), o.state(0).astype(np.float32))
+    gw = sim.weights()["weight"]
+    assert np.array_equal(gw, o.weights()[0].astype(np.float32))
+
+
+def test_conductance_izhikevich_kat_on_gpu():
+    import json
+    import os
+
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "numerical_accuracy_kat.json")))
+    net = nb.Network().add_layer(nb.NeuronLayer("TimeDrivenIzhikevic_Exponential_Decay", 1, output=True))
+    sim = nb.Simulation(net, nb.SimulationConfig(steps=24, timestep=gold["timestep"]))
+    sim.set_current_at(1, 0, gold["current"])
+    v, u = [], []
+    for _ in range(gold["steps"]):
+        sim.run(1)
+        st = sim.neuron_state(0)["state_variables"]
+        v.append(st[0])
+        u.append(st[1])
+    assert np.array_equal(np.float32(v), np.float32(gold["izhikevich"]["expected_v"]))
+    assert np.array_equal(np.float32(u), np.float32(gold["izhikevich"]["expected_u"]))
+
+
+def test_dense_semantics_profile(oracle_lib):
+    net, cfg = workloads.plain_lif(n=300, steps=2000)
+    sim = nb.Simulation(net, cfg, semantics="dense")
+    sim.run()
+    o = _oracle(net, cfg, semantics=1)
+    o.run(cfg.steps)
+    assert _raster_equal(sim.spike_raster(), _oracle_raster(o))
+    assert np.array_equal(sim.state_field(0), o.state(0).astype(np.float32))
+
+
+def test_run_calls_compose():
+    net, cfg = workloads.plain_lif(n=400, steps=1000)
+    a = nb.Simulation(net, cfg)
+    a.run(300).run(200).run(1)
+    b = nb.Simulation(net, cfg)
+    b.run(501)
+    assert a.next_time == b.next_time == 502
+    assert _raster_equal(a.spike_raster(), b.spike_raster())
+    assert np.array_equal(a.state_field(0), b.state_field(0))
+
+
+def test_launch_shape_invariance():
+    net, cfg = workloads.izhikevich_stdp(n=4000, in_degree=50)
+    ref = nb.Simulation(net, cfg, seed=2)
+    ref.run(1500)
+    for kw in ({"block_steps": 1}, {"block_steps": 3, "threads_per_block": 64}, {"use_graph": False}):
+        s = nb.Simulation(net, cfg, seed=2, **kw)
+        s.run(1500)
+        assert _raster_equal(ref.spike_raster(), s.spike_raster()), kw
+        assert np.array_equal(ref.weights()["weight"], s.weights()["weight"]), kw
+
+
+def test_batched_union_equals_independent_instances():
+    singles, union, cfg = workloads.batched_lif(instances=6, lo=200, hi=3000, steps=500)
+    u = nb.Simulation(union, cfg)
+    u.run(500)
+    ut, ui = u.spike_raster()
+    offset = 0
+    for net in singles:
+        n = net.neuron_count
+        s = nb.Simulation(net, cfg)
+        s.run(500)
+        sel = (ui >= offset) & (ui < offset + n)
+        assert _raster_equal((ut[sel], ui[sel] - offset), s.spike_raster())
+        offset += n
+
+
+def test_reset_restores_initial_state():
+    net, cfg = workloads.plain_lif(n=200, steps=300)
+    s = nb.Simulation(net, cfg)
+    s.run()
+    r1 = s.spike_raster()
+    s.reset()
+    s.run()
+    assert _raster_equal(r1, s.spike_raster())
+
+
+def test_weight_get_set_by_original_index():
+    net, cfg = workloads.plain_lif(n=100, steps=10)
+    s = nb.Simulation(net, cfg)
+    w0 = net.to_native().weight
+    assert s.get_connection_weight(5) == w0[5]
+    s.set_connection_weight(5, 1.25)
+    assert s.get_connection_weight(5) == np.float32(1.25)
+    with pytest.raises(nb.NbgError):
+        s.set_connection_weight(10**9, 1.0)
