@@ -84,6 +84,7 @@ typedef struct {
     int count;
     float f[NBG_NFP];
     int ip[NBG_NIP];
+    int output; /* record this layer's spikes (NeuronLayer.output) */
 } nbg_layer_desc;
 
 /* Pair STDP parameters (STDP::SetParameters keys Max_LTP, LTP_tau, Max_LTD,
@@ -158,7 +159,9 @@ enum {
 nbg_status nbg_get_state(nbg_engine *e, int field, float *out /* n_neurons */);
 nbg_status nbg_set_state(nbg_engine *e, int field, const float *in /* n_neurons */);
 
-/* Spikes recorded by all run calls so far, ordered by (time, neuron id). */
+/* Spikes of output layers recorded by all run calls so far, ordered by
+ * (time, neuron id) -- the reference's output spike buffer
+ * (ArrayOutputSpikeDriver, read by _core.Simulation.output_spikes). */
 nbg_status nbg_num_spikes(nbg_engine *e, int64_t *n);
 nbg_status nbg_get_spikes(nbg_engine *e, int32_t *times, int32_t *ids, int64_t capacity);
 nbg_status nbg_clear_spikes(nbg_engine *e);
@@ -175,6 +178,10 @@ nbg_status nbg_set_weight(nbg_engine *e, int64_t conn, float w);
  * target's total current, e.g. TimeDrivenLIF_Voltage_jump.cpp:117-124;
  * PROPOGATEDCURRENT outranks PROPOGATEDSPIKE, Event.h:10). */
 nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value);
+/* A PoissonRate layer without incoming synapses is a generator: its spikes
+ * are a pure function of (local index, step), so targets evaluate them inline
+ * instead of through the delay ring.  Timed currents into generator neurons
+ * are rejected with NBG_ERR_UNSUPPORTED. */
 
 /* Membrane (field 0) traces of selected neurons, one row per update. */
 nbg_status nbg_set_trace(nbg_engine *e, int n, const int32_t *ids);

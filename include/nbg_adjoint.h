@@ -1,0 +1,62 @@
+/*
+ * nbg_adjoint.h -- fused elementwise kernels of a differentiable recurrent
+ * voltage-jump LIF network, forward step and hand-written adjoint step.
+ * Pointers are device pointers; `stream` is a cudaStream_t (NULL = default).
+ *
+ * There is no counterpart in the reference: it has no gradient path.  The
+ * neuron is the reference's voltage-jump LIF (TimeDrivenLIF_Voltage_jump.cpp
+ * :49-113) written as a differentiable recurrence, one step of dt:
+ *
+ *   m_t = (ref_{t-1} == 0)                                  integrating
+ *   u_t = m_t ? v_{t-1} + alpha (V_rest - v_{t-1}) + I_t : V_reset
+ *   s_t = H(u_t - theta)        spiking mode   (surrogate 1/(1+k|u-theta|)^2)
+ *       = sigmoid(k (u_t - theta))  smoothed mode (exact derivative)
+ *   v_t = u_t - s_t (u_t - V_reset)
+ *   ref_t = s_t ? t_ref : max(ref_{t-1} - 1, 0)             (spiking mode)
+ *   z    += c_t s_t                                         readout weight
+ *
+ * with I_t = x_t W_in + s_{t-1} W_rec computed by the caller, alpha = dt/tau
+ * and theta per neuron.  The adjoint step receives g_ext = dL/ds_t from the
+ * recurrent path (dI_{t+1} W_rec^T), adds c_t * g_read (the readout term),
+ * and returns dI_t = dL/dI_t, the running lambda_v = dL/dv_{t-1}, and
+ * accumulates dL/dtheta and dL/dalpha per (instance, neuron).
+ */
+#ifndef NBG_ADJOINT_H
+#define NBG_ADJOINT_H
+
+#include "nbg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    float v_rest, v_reset, slope;
+    int t_ref;  /* refractory steps (spiking mode) */
+    int smooth; /* 0: Heaviside spikes + fast-sigmoid surrogate; 1: sigmoid spikes */
+} nbg_lif_grad_params;
+
+/* One forward step over B x N neurons.  u_rec, m_rec, vprev_rec (optional,
+ * NULL to skip) record u_t, m_t and v_{t-1} for the adjoint; s_out receives
+ * s_t; z += c_t * s_t. */
+nbg_status nbg_lif_forward_step(const float *I, float *v, int32_t *ref, float *s_out, float *u_rec, uint8_t *m_rec,
+                                float *vprev_rec, float *z, float c_t, const float *alpha, const float *theta,
+                                const nbg_lif_grad_params *p, int B, int N, void *stream);
+
+/* One adjoint step (reverse time).  g_ext may be NULL (last step). */
+nbg_status nbg_lif_adjoint_step(const float *g_ext, const float *g_read, float c_t, const float *u, const float *s,
+                                const uint8_t *m, const float *vprev, float *lam_v, float *dI, float *g_theta,
+                                float *g_alpha, const float *alpha, const float *theta, const nbg_lif_grad_params *p,
+                                int B, int N, void *stream);
+
+/* Poisson input spikes x[t][b][c] in {0, 1}: channel c fires with
+ * probability min(1, rate_c * dt * 1e-3) from the PoissonRate hash of
+ * (seed-offset index b*C + c + seed, step t). */
+nbg_status nbg_poisson_inputs(float *x, const float *rates_hz, int T, int B, int C, float dt_ms, int seed,
+                              void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBG_ADJOINT_H */

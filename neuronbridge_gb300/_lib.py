@@ -35,7 +35,7 @@ STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "OOM", 4: "OVERFLOW", 5: "STATE",
 
 class LayerDesc(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int), ("count", ctypes.c_int), ("f", ctypes.c_float * NFP),
-                ("ip", ctypes.c_int * NIP)]
+                ("ip", ctypes.c_int * NIP), ("output", ctypes.c_int)]
 
 
 class StdpDesc(ctypes.Structure):

@@ -21,8 +21,10 @@ LIB = os.path.join(BUILD, "libnbg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction, so every float operation rounds
 # once exactly as in the CPU oracle and the reference's scalar C++.
+# -Xcompiler -ffp-contract=off: the same for host code (gcc contracts a*b+c into
+# fma by default on aarch64).
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

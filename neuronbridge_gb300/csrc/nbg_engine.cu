@@ -47,13 +47,14 @@
 #include <string>
 #include <vector>
 
-#include "../../include/nbg.h"
+#include "nbg.h"
+#include "nbg_common.cuh"
 
 namespace {
-
 thread_local std::string g_err;
+}
 
-nbg_status fail(nbg_status code, const char *fmt, ...) {
+nbg_status nbg_fail(nbg_status code, const char *fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -63,13 +64,13 @@ nbg_status fail(nbg_status code, const char *fmt, ...) {
     return code;
 }
 
-#define NBG_CUDA(call)                                                                         \
-    do {                                                                                       \
-        cudaError_t e_ = (call);                                                               \
-        if (e_ != cudaSuccess)                                                                 \
-            return fail(e_ == cudaErrorMemoryAllocation ? NBG_ERR_OOM : NBG_ERR_CUDA,          \
-                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-    } while (0)
+namespace {
+
+inline nbg_status fail(nbg_status code, const char *msg) { return nbg_fail(code, "%s", msg); }
+template <typename... A>
+inline nbg_status fail(nbg_status code, const char *fmt, A... a) {
+    return nbg_fail(code, fmt, a...);
+}
 
 constexpr int kMaxBlockSteps = 32;
 constexpr int kErrOverflow = 1;
@@ -79,6 +80,8 @@ constexpr int kErrEventLog = 2;
 
 struct LayerDev {
     int model, start, count, has_exc, has_inh;
+    int record;    // output layer: spikes go to the raster
+    int generator; // source-free PoissonRate: targets evaluate its spikes inline
     float f[NBG_NFP];
     int ip[NBG_NIP];
     float decay_exc, decay_inh; // IZH_COND conductance decay per step
@@ -106,6 +109,9 @@ struct NetDev {
     const int *out_ptr;
     const unsigned int *out_bit;
     const unsigned short *out_delay;
+    // in-synapses from generator layers, per target, sorted by CSC rank
+    const int *gen_ptr, *gen_pos, *gen_src;
+    const unsigned short *gen_delay;
     int *blk_spk, *blk_cnt;
     int *out_ids, *out_cnt;
     long long *cursor;
@@ -124,15 +130,12 @@ struct NetDev {
 };
 
 __device__ __forceinline__ float hash_uniform01(int neuron_index, int time_step) {
-    unsigned int x = (unsigned int)neuron_index * 747796405u + (unsigned int)(time_step + 1) * 2891336453u +
-                     0x9e3779b9u;
-    x ^= x >> 16;
-    x *= 2246822519u;
-    x ^= x >> 13;
-    x *= 3266489917u;
-    x ^= x >> 16;
-    return (float)(x & 0x00FFFFFFu) / (float)0x01000000u;
+    return nbg_hash_uniform01(neuron_index, time_step);
 }
+
+// Spike of generator neuron k at step ts (PoissonRate::UpdateState with no
+// inputs: the rate is bias + gain * I_ext, identical to update_neuron below).
+__device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts);
 
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
     z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
@@ -163,17 +166,43 @@ struct NeuronRegs {
     int last;
 };
 
-// STDP trace decay to time t (STDP_State::SetUpdate) from the host table.
-__device__ __forceinline__ void stdp_decay(const NetDev &n, int s, int rule, int t) {
-    int k = t - n.slast[s];
-    float fp = 0.0f, fm = 0.0f;
-    if (k < n.dtab_len) {
-        fp = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + k]);
-        fm = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + k]);
+// Per-thread copy of the parameters its neuron's model uses (a compact
+// subset of LayerDev, to keep the update kernel's register count low).
+//   LIF_VJ   p: V_rest tau V_th R V_reset alpha        ip: t_ref
+//   IZH_COND p: a b c d V_th R E_ampa E_gaba dexc dinh  flags: has_exc has_inh
+//   IZH_RK4  p: a b c d V_th sigma
+//   POISSON  p: rate_bias gain                         ip: layer start
+struct Model {
+    int model, ip, flags, record;
+    float p[10];
+};
+
+__device__ __forceinline__ Model load_model(const LayerDev &L) {
+    Model m;
+    m.model = L.model;
+    m.record = L.record;
+    m.ip = 0;
+    m.flags = (L.has_exc ? 1 : 0) | (L.has_inh ? 2 : 0);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m.p[k] = 0.0f;
+    switch (L.model) {
+    case NBG_MODEL_LIF_VJ:
+        m.p[0] = L.f[0]; m.p[1] = L.f[1]; m.p[2] = L.f[2]; m.p[3] = L.f[3]; m.p[4] = L.f[4]; m.p[5] = L.alpha;
+        m.ip = L.ip[0];
+        break;
+    case NBG_MODEL_IZH_COND:
+        m.p[0] = L.f[0]; m.p[1] = L.f[1]; m.p[2] = L.f[2]; m.p[3] = L.f[3]; m.p[4] = L.f[5]; m.p[5] = L.f[6];
+        m.p[6] = L.f[7]; m.p[7] = L.f[9]; m.p[8] = L.decay_exc; m.p[9] = L.decay_inh;
+        break;
+    case NBG_MODEL_IZH_RK4:
+        m.p[0] = L.f[0]; m.p[1] = L.f[1]; m.p[2] = L.f[2]; m.p[3] = L.f[3]; m.p[4] = L.f[5]; m.p[5] = L.f[6];
+        break;
+    default:
+        m.p[0] = L.f[0]; m.p[1] = L.f[1];
+        m.ip = L.start;
+        break;
     }
-    n.apre[s] = n.apre[s] * fp;
-    n.apost[s] = n.apost[s] * fm;
-    n.slast[s] = t;
+    return m;
 }
 
 __device__ __forceinline__ float clamp_w(float w, float wmax) {
@@ -182,14 +211,44 @@ __device__ __forceinline__ float clamp_w(float w, float wmax) {
     return w;
 }
 
+// Pair STDP on synapse s at step t (L/LearningRule/src/Rule/STDP.cpp:19-61,
+// State/STDP_State.cpp:17-26): decay both traces from the host table by the
+// integer step gap, then the pre (Apre += 1, w -= A- Apost) or post
+// (Apost += 1, w += A+ Apre) jump and the clamp to [0, wmax].  All loads of
+// the synapse are independent and issued together.
+template <bool kPre>
+__device__ __forceinline__ void stdp_update(const NetDev &n, int s, int rule, int t, float w) {
+    const int last = n.slast[s];
+    const float apre = n.apre[s], apost = n.apost[s], wmax = n.wmax[s];
+    const float a = __ldg(&n.rule_a[rule * 2 + (kPre ? 1 : 0)]);
+    const int k = t - last;
+    float fp = 0.0f, fm = 0.0f;
+    if (k < n.dtab_len) {
+        fp = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + k]);
+        fm = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + k]);
+    }
+    float xpre = apre * fp, xpost = apost * fm;
+    if (kPre) {
+        xpre = xpre + 1.0f;
+        w = clamp_w(w + (-a * xpost), wmax);
+    } else {
+        xpost = xpost + 1.0f;
+        w = clamp_w(w + a * xpre, wmax);
+    }
+    n.apre[s] = xpre;
+    n.apost[s] = xpost;
+    n.slast[s] = t;
+    n.w[s] = w;
+}
+
 // Apply one arrival (ProcessSpike of the target model), then the pre hook.
-__device__ __forceinline__ void apply_arrival(const NetDev &n, const LayerDev &L, NeuronRegs &r, float &acc_a,
+__device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
                                               float &acc_b, bool gate, int s, int t) {
     const unsigned char meta = n.meta[s];
+    const float w = n.w[s];
     const int type = meta & 1;
     const int rule = (int)(meta >> 1) - 1;
-    const float w = n.w[s];
-    switch (L.model) {
+    switch (M.model) {
     case NBG_MODEL_LIF_VJ:
         if (n.semantics == NBG_SEM_DENSE) {
             if (type == 0) acc_a = acc_a + w;
@@ -216,25 +275,21 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const LayerDev &L
             atomicOr(n.err, kErrEventLog);
         }
     }
-    if (rule >= 0) {
-        stdp_decay(n, s, rule, t);
-        n.apre[s] = n.apre[s] + 1.0f;
-        const float am = __ldg(&n.rule_a[rule * 2 + 1]);
-        n.w[s] = clamp_w(w + (-am * n.apost[s]), n.wmax[s]);
-    }
+    if (rule >= 0) stdp_update<true>(n, s, rule, t, w);
 }
 
-// One neuron update; returns true on a spike.
-__device__ __forceinline__ bool update_neuron(const NetDev &n, const LayerDev &L, NeuronRegs &r, float acc_a,
-                                             float acc_b, int j, int t) {
-    switch (L.model) {
+// One neuron update; returns true on a spike.  `noise` is
+// sigma * gauss12(seed, j, t) for noisy IZH_RK4 layers (else 0).
+__device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, NeuronRegs &r, float acc_a,
+                                             float acc_b, float noise, int j, int t) {
+    switch (M.model) {
     case NBG_MODEL_LIF_VJ: {
         if (n.semantics == NBG_SEM_DENSE) {
             float nv = r.v + acc_a - acc_b;
-            if (r.last >= L.ip[0]) nv = nv + L.alpha * (L.f[0] - nv + L.f[3] * r.iext);
+            if (r.last >= M.ip) nv = nv + M.p[5] * (M.p[0] - nv + M.p[3] * r.iext);
             r.last += 1;
-            if (nv >= L.f[2]) {
-                r.v = L.f[4];
+            if (nv >= M.p[2]) {
+                r.v = M.p[4];
                 r.last = 0;
                 return true;
             }
@@ -242,12 +297,12 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const LayerDev &L
             return false;
         }
         float cur = 0.0f;
-        cur = cur + L.f[3] * r.iext / L.f[1];
-        float aux = (r.last > L.ip[0]) ? cur + (L.f[0] - r.v) / L.f[1] : 0.0f;
+        cur = cur + M.p[3] * r.iext / M.p[1];
+        float aux = (r.last > M.ip) ? cur + (M.p[0] - r.v) / M.p[1] : 0.0f;
         r.v = r.v + aux * n.dt;
         r.last += 1;
-        if (r.v > L.f[2]) {
-            r.v = L.f[4];
+        if (r.v > M.p[2]) {
+            r.v = M.p[4];
             r.last = 0;
             return true;
         }
@@ -256,31 +311,31 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const LayerDev &L
     case NBG_MODEL_IZH_COND: {
         const float V = r.v, U = r.u;
         float total = 0.0f;
-        if (L.has_exc) total = total + r.gexc * (L.f[7] - V);
-        if (L.has_inh) total = total + r.ginh * (L.f[9] - V);
+        if (M.flags & 1) total = total + r.gexc * (M.p[6] - V);
+        if (M.flags & 2) total = total + r.ginh * (M.p[7] - V);
         total = total + r.iext;
         float dv = 0.0f, du = 0.0f;
         if (r.last > 0) {
-            dv = 0.04f * V * V + 5.0f * V + 140.0f - U + L.f[6] * total;
-            du = L.f[0] * (L.f[1] * V - U);
+            dv = 0.04f * V * V + 5.0f * V + 140.0f - U + M.p[5] * total;
+            du = M.p[0] * (M.p[1] * V - U);
         }
         r.v = r.v + dv * n.dt;
         r.u = r.u + du * n.dt;
-        if (L.has_exc) r.gexc = r.gexc * L.decay_exc;
-        if (L.has_inh) r.ginh = r.ginh * L.decay_inh;
+        if (M.flags & 1) r.gexc = r.gexc * M.p[8];
+        if (M.flags & 2) r.ginh = r.ginh * M.p[9];
         r.last += 1;
-        if (r.v >= L.f[5]) {
-            r.v = L.f[2];
-            r.u = r.u + L.f[3];
+        if (r.v >= M.p[4]) {
+            r.v = M.p[2];
+            r.u = r.u + M.p[3];
             r.last = 0;
             return true;
         }
         return false;
     }
     case NBG_MODEL_IZH_RK4: {
-        const float a = L.f[0], b = L.f[1];
+        const float a = M.p[0], b = M.p[1];
         float I = acc_a + r.iext;
-        if (L.f[6] != 0.0f) I = I + L.f[6] * gauss12(n.seed, j, t);
+        if (M.p[5] != 0.0f) I = I + noise;
         if (r.last > 0) {
             const float h = n.dt, hh = 0.5f * n.dt, h6 = n.dt / 6.0f;
             const float v = r.v, u = r.u;
@@ -295,20 +350,20 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const LayerDev &L
             r.u = u + h6 * (k1u + 2.0f * k2u + 2.0f * k3u + k4u);
         }
         r.last += 1;
-        if (r.v >= L.f[5]) {
-            r.v = L.f[2];
-            r.u = r.u + L.f[3];
+        if (r.v >= M.p[4]) {
+            r.v = M.p[2];
+            r.u = r.u + M.p[3];
             r.last = 0;
             return true;
         }
         return false;
     }
     default: { // POISSON
-        float rate = L.f[0] + acc_a + L.f[1] * r.iext;
+        float rate = M.p[0] + acc_a + M.p[1] * r.iext;
         rate = rate > 0.0f ? rate : 0.0f;
         float prob = rate * n.dt * 0.001f;
         prob = prob < 1.0f ? prob : 1.0f;
-        if (hash_uniform01(j - L.start, t) < prob) {
+        if (hash_uniform01(j - M.ip, t) < prob) {
             r.last = 0;
             return true;
         }
@@ -318,21 +373,40 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const LayerDev &L
     }
 }
 
+__device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts) {
+    if (ts < 0) return false;
+    const LayerDev &G = n.layers[n.pop[k]];
+    float rate = G.f[0] + 0.0f + G.f[1] * n.iext[k];
+    rate = rate > 0.0f ? rate : 0.0f;
+    float prob = rate * n.dt * 0.001f;
+    prob = prob < 1.0f ? prob : 1.0f;
+    return hash_uniform01(k - G.start, ts) < prob;
+}
+
 // Advance every neuron B steps (drain arrivals, integrate, compact spikes,
 // post-synaptic STDP).  One thread per neuron; all lanes stay in the loop so
-// the per-step warp ballot is full-warp.
-__global__ void __launch_bounds__(256) k_update(NetDev n, int B) {
+// the per-step warp collectives are full-warp.
+//   * the noise currents of the block are drawn up front (independent hash
+//     chains, so they overlap instead of lengthening the per-step chain);
+//   * the first kPrefetch mask words of step b+1 are loaded while step b runs
+//     (every mark for the block's slots was made by earlier launches);
+//   * the post-synaptic STDP pass of a spiking neuron is spread over its warp:
+//     the 32 lanes stride over that neuron's CSC list.
+constexpr int kPrefetch = 4;
+
+__global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = j < n.N;
     const int lane = threadIdx.x & 31;
     const int T0 = *n.tnow;
     const int run_t0 = *n.run_t0;
 
-    LayerDev L;
+    Model L;
     NeuronRegs r;
-    int base = 0, woff = 0, nw = 0, tslot = -1;
+    int base = 0, end = 0, woff = 0, nw = 0, tslot = -1, g0 = 0, g1 = 0;
+    bool listed = false;
     if (active) {
-        L = n.layers[n.pop[j]];
+        L = load_model(n.layers[n.pop[j]]);
         r.v = n.v[j];
         r.u = n.u[j];
         r.gexc = n.gexc[j];
@@ -340,22 +414,62 @@ __global__ void __launch_bounds__(256) k_update(NetDev n, int B) {
         r.iext = n.iext[j];
         r.last = n.last[j];
         base = n.csc_ptr[j];
+        end = n.csc_ptr[j + 1];
         woff = n.woff[j];
         nw = n.woff[j + 1] - woff;
         if (n.trace_slot) tslot = n.trace_slot[j];
+        g0 = n.gen_ptr[j];
+        g1 = n.gen_ptr[j + 1];
+        // compacted if its spikes are recorded or must be propagated
+        listed = L.record || n.out_ptr[j + 1] > n.out_ptr[j];
+    }
+    float nz[kMaxBlockSteps];
+    if (active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f) {
+#pragma unroll 4
+        for (int b = 0; b < B; ++b) nz[b] = L.p[5] * gauss12(n.seed, j, T0 + b);
+    }
+    const int npre = nw < kPrefetch ? nw : kPrefetch;
+    unsigned int nxt[kPrefetch] = {0u, 0u, 0u, 0u};
+    if (active) {
+        const unsigned int *row0 = n.mask + (size_t)((unsigned int)T0 % (unsigned int)n.D) * n.Wt + woff;
+#pragma unroll
+        for (int k = 0; k < kPrefetch; ++k)
+            if (k < npre) nxt[k] = row0[k];
     }
     unsigned long long delivered = 0;
     for (int b = 0; b < B; ++b) {
         const int t = T0 + b;
         bool spk = false;
         if (active) {
-            float acc_a = 0.0f, acc_b = 0.0f;
-            const bool gate = r.last > L.ip[0];
+            unsigned int cur[kPrefetch];
+#pragma unroll
+            for (int k = 0; k < kPrefetch; ++k) cur[k] = nxt[k];
             unsigned int *mrow = n.mask + (size_t)((unsigned int)t % (unsigned int)n.D) * n.Wt + woff;
+            if (b + 1 < B) {
+                const unsigned int *mnext = n.mask + (size_t)((unsigned int)(t + 1) % (unsigned int)n.D) * n.Wt + woff;
+#pragma unroll
+                for (int k = 0; k < kPrefetch; ++k)
+                    if (k < npre) nxt[k] = mnext[k];
+            }
+            float acc_a = 0.0f, acc_b = 0.0f;
+            const bool gate = r.last > L.ip;
+            int gq = g0;
             for (int wi = 0; wi < nw; ++wi) {
-                unsigned int word = mrow[wi];
+                unsigned int word;
+                if (wi < kPrefetch) {
+                    word = cur[0];
+#pragma unroll
+                    for (int k = 1; k < kPrefetch; ++k)
+                        if (wi == k) word = cur[k];
+                } else {
+                    word = mrow[wi];
+                }
+                if (word) mrow[wi] = 0u;
+                // generator arrivals of this word, evaluated inline
+                for (; gq < g1 && (n.gen_pos[gq] >> 5) == wi; ++gq)
+                    if (generator_fired(n, n.gen_src[gq], t - (int)n.gen_delay[gq]))
+                        word |= 1u << (n.gen_pos[gq] & 31);
                 if (!word) continue;
-                mrow[wi] = 0u;
                 delivered += __popc(word);
                 while (word) {
                     const int p = wi * 32 + __ffs(word) - 1;
@@ -363,30 +477,31 @@ __global__ void __launch_bounds__(256) k_update(NetDev n, int B) {
                     apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
                 }
             }
-            spk = update_neuron(n, L, r, acc_a, acc_b, j, t);
+            spk = update_neuron(n, L, r, acc_a, acc_b, nz[b], j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
         }
-        const unsigned int bal = __ballot_sync(0xffffffffu, spk);
+        const unsigned int bal = __ballot_sync(0xffffffffu, spk && listed);
         if (bal) {
             const int leader = __ffs(bal) - 1;
             int pos = 0;
             if (lane == leader) pos = atomicAdd(&n.blk_cnt[b], __popc(bal));
             pos = __shfl_sync(0xffffffffu, pos, leader);
-            if (spk) {
-                n.blk_spk[(size_t)b * n.N + pos + __popc(bal & ((1u << lane) - 1u))] = j;
-                // post-synaptic STDP over this neuron's plastic in-synapses
-                const int end = n.csc_ptr[j + 1];
-                for (int s = base; s < end; ++s) {
-                    const unsigned char meta = n.meta[s];
-                    if (meta < 2) continue;
-                    const int rule = (int)(meta >> 1) - 1;
-                    stdp_decay(n, s, rule, t);
-                    n.apost[s] = n.apost[s] + 1.0f;
-                    const float ap = __ldg(&n.rule_a[rule * 2 + 0]);
-                    n.w[s] = clamp_w(n.w[s] + ap * n.apre[s], n.wmax[s]);
-                }
+            if (spk && listed) n.blk_spk[(size_t)b * n.N + pos + __popc(bal & ((1u << lane) - 1u))] = j;
+        }
+        // post-synaptic STDP (STDP::ApplyPostSynaticSpike) of every spiking
+        // lane, the warp striding over that neuron's in-synapses
+        unsigned int sbal = __ballot_sync(0xffffffffu, spk && end > base);
+        while (sbal) {
+            const int l = __ffs(sbal) - 1;
+            sbal &= sbal - 1u;
+            const int s0 = __shfl_sync(0xffffffffu, base, l), s1 = __shfl_sync(0xffffffffu, end, l);
+            for (int s = s0 + lane; s < s1; s += 32) {
+                const unsigned char meta = n.meta[s];
+                if (meta < 2) continue;
+                stdp_update<false>(n, s, (int)(meta >> 1) - 1, t, n.w[s]);
             }
         }
+        __syncwarp(); // the owners read these synapses at their next arrivals
     }
     if (active) {
         n.v[j] = r.v;
@@ -427,7 +542,8 @@ __global__ void __launch_bounds__(256) k_propagate(NetDev n, int B) {
         const int src = n.blk_spk[(size_t)b * n.N + (g - pre[b])];
         const unsigned int t = (unsigned int)(T0 + b);
         if (lane == 0) {
-            if (cur + g < n.out_cap) n.out_ids[cur + g] = src;
+            // non-output neurons keep their slot as -1 (dropped on the host)
+            if (cur + g < n.out_cap) n.out_ids[cur + g] = n.layers[n.pop[src]].record ? src : -1;
             else atomicOr(n.err, kErrOverflow);
         }
         const int q0 = n.out_ptr[src], q1 = n.out_ptr[src + 1];
@@ -455,30 +571,6 @@ __global__ void __launch_bounds__(256) k_propagate(NetDev n, int B) {
 
 // ------------------------------------------------------------------ host side
 
-template <typename T>
-struct DevBuf {
-    T *p = nullptr;
-    size_t n = 0;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    cudaError_t alloc(size_t count) {
-        release();
-        n = count;
-        if (count == 0) return cudaSuccess;
-        return cudaMalloc(&p, count * sizeof(T));
-    }
-    cudaError_t upload(const std::vector<T> &h) {
-        cudaError_t e = alloc(h.size());
-        if (e != cudaSuccess || h.empty()) return e;
-        return cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
-    }
-    cudaError_t zero() { return n ? cudaMemset(p, 0, n * sizeof(T)) : cudaSuccess; }
-};
-
 } // namespace
 
 struct nbg_engine {
@@ -496,6 +588,7 @@ struct nbg_engine {
     int64_t ev_cap = 0;
     // host copies
     std::vector<LayerDev> layers;
+    std::vector<unsigned short> pop_host;
     std::vector<int> csc_ptr;
     std::vector<int64_t> csc_orig; // CSC position -> original connection index
     std::vector<int64_t> orig_pos; // original connection index -> CSC position
@@ -507,6 +600,8 @@ struct nbg_engine {
     DevBuf<unsigned char> meta;
     DevBuf<LayerDev> d_layers;
     DevBuf<float> v, u, gexc, ginh, iext, w, wmax, apre, apost, dtab, rule_a, trace, ev_w;
+    DevBuf<int> gen_ptr, gen_pos, gen_src;
+    DevBuf<unsigned short> gen_delay;
     DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, blk_spk, blk_cnt, out_ids, out_cnt, err, tnow, run_t0,
         trace_slot, ev_t, ev_pos;
     DevBuf<unsigned int> mask, out_bit, done;
@@ -575,6 +670,10 @@ struct nbg_engine {
         n.out_ptr = out_ptr.p;
         n.out_bit = out_bit.p;
         n.out_delay = out_delay.p;
+        n.gen_ptr = gen_ptr.p;
+        n.gen_pos = gen_pos.p;
+        n.gen_src = gen_src.p;
+        n.gen_delay = gen_delay.p;
         n.blk_spk = blk_spk.p;
         n.blk_cnt = blk_cnt.p;
         n.out_ids = out_ids.p;
@@ -679,13 +778,16 @@ constexpr int kGraphBlocks = 64;
 
 // Launch one block of B steps.  With kernel timing, `slot` selects the event
 // triple bracketing the two kernels.
-void launch_block(nbg_engine *e, const NetDev &nd, int B, int slot) {
+// Inside stream capture an event record must be "external" to become an
+// event-record node of the graph (a plain record is only a dependency).
+void launch_block(nbg_engine *e, const NetDev &nd, int B, int slot, bool capturing = false) {
     const int grid = (e->N + e->threads - 1) / e->threads;
-    if (e->kernel_timing) cudaEventRecord(e->tev[3 * slot + 0], e->stream);
+    const unsigned int flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 0], e->stream, flags);
     k_update<<<grid, e->threads, 0, e->stream>>>(nd, B);
-    if (e->kernel_timing) cudaEventRecord(e->tev[3 * slot + 1], e->stream);
+    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 1], e->stream, flags);
     k_propagate<<<e->prop_grid, 256, 0, e->stream>>>(nd, B);
-    if (e->kernel_timing) cudaEventRecord(e->tev[3 * slot + 2], e->stream);
+    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 2], e->stream, flags);
 }
 
 // Sum the bracketed kernel durations of `blocks` event triples.
@@ -784,6 +886,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
         L.model = ld.model;
         L.start = start;
         L.count = ld.count;
+        L.record = ld.output != 0;
         std::memcpy(L.f, ld.f, sizeof(L.f));
         std::memcpy(L.ip, ld.ip, sizeof(L.ip));
         if (ld.model == NBG_MODEL_IZH_COND) {
@@ -841,13 +944,23 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
                              d->rule[s]));
         if (!std::isfinite(d->weight[s]) || !std::isfinite(d->max_weight[s]))
             return bail(fail(NBG_ERR_INVALID, "connection %lld: weight must be finite", (long long)s));
-        e->dmin = std::min(e->dmin, d->delay[s]);
-        e->dmax = std::max(e->dmax, d->delay[s]);
         indeg[b + 1]++;
         if (d->type[s] == 0) e->layers[pop[b]].has_exc = 1;
         else e->layers[pop[b]].has_inh = 1;
     }
-    if (S == 0) e->dmin = kMaxBlockSteps;
+    // generator layers: PoissonRate layers without incoming synapses
+    {
+        std::vector<int64_t> layer_in(d->n_layers, 0);
+        for (int i = 0; i < e->N; ++i) layer_in[pop[i]] += indeg[i + 1];
+        for (int l = 0; l < d->n_layers; ++l)
+            e->layers[l].generator = e->layers[l].model == NBG_MODEL_POISSON && layer_in[l] == 0;
+    }
+    for (int64_t s = 0; s < S; ++s) {
+        if (e->layers[pop[d->source[s]]].generator) continue;
+        e->dmin = std::min(e->dmin, d->delay[s]);
+        e->dmax = std::max(e->dmax, d->delay[s]);
+    }
+    if (e->dmin == 0x7FFFFFFF) e->dmin = kMaxBlockSteps; // nothing goes through the ring
     std::vector<int> &cptr = e->csc_ptr;
     cptr.assign((size_t)e->N + 1, 0);
     for (int i = 0; i < e->N; ++i) cptr[i + 1] = cptr[i] + indeg[i + 1];
@@ -872,6 +985,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     for (int j = 0; j < e->N; ++j) woff[j + 1] = woff[j] + (cptr[j + 1] - cptr[j] + 31) / 32;
     e->Wt = std::max(woff[e->N], 1);
     e->D = e->dmax + 1;
+    e->pop_host = pop;
     std::vector<float> w((size_t)S), wmax((size_t)S);
     std::vector<unsigned char> meta((size_t)S);
     std::vector<int> src_of((size_t)S);
@@ -884,19 +998,38 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     }
     e->init_w = w;
 
-    // ---- CSR by source over (mask bit, delay)
+    // ---- CSR by source over (mask bit, delay); generator sources excluded
     std::vector<int> optr((size_t)e->N + 1, 0);
-    for (int64_t p = 0; p < S; ++p) optr[src_of[p] + 1]++;
-    for (int i = 0; i < e->N; ++i) optr[i + 1] += optr[i];
-    std::vector<unsigned int> obit((size_t)S);
-    std::vector<unsigned short> odelay((size_t)S);
+    std::vector<int> gptr((size_t)e->N + 1, 0);
+    for (int j = 0; j < e->N; ++j)
+        for (int p = cptr[j]; p < cptr[j + 1]; ++p) {
+            if (e->layers[pop[src_of[p]]].generator) gptr[j + 1]++;
+            else optr[src_of[p] + 1]++;
+        }
+    for (int i = 0; i < e->N; ++i) {
+        optr[i + 1] += optr[i];
+        gptr[i + 1] += gptr[i];
+    }
+    std::vector<unsigned int> obit((size_t)optr[e->N]);
+    std::vector<unsigned short> odelay((size_t)optr[e->N]);
+    std::vector<int> gpos((size_t)gptr[e->N]), gsrc((size_t)gptr[e->N]);
+    std::vector<unsigned short> gdelay((size_t)gptr[e->N]);
     {
         std::vector<int> fill(optr.begin(), optr.end() - 1);
+        int gq = 0;
         for (int j = 0; j < e->N; ++j)
             for (int p = cptr[j]; p < cptr[j + 1]; ++p) {
+                const unsigned short dl = (unsigned short)d->delay[e->csc_orig[p]];
+                if (e->layers[pop[src_of[p]]].generator) {
+                    gpos[gq] = p - cptr[j]; // ascending within j: CSC order
+                    gsrc[gq] = src_of[p];
+                    gdelay[gq] = dl;
+                    ++gq;
+                    continue;
+                }
                 const int q = fill[src_of[p]]++;
                 obit[q] = (unsigned int)woff[j] * 32u + (unsigned int)(p - cptr[j]);
-                odelay[q] = (unsigned short)d->delay[e->csc_orig[p]];
+                odelay[q] = dl;
             }
     }
     if ((uint64_t)e->Wt * 32ull > 0xFFFFFFFFull) return bail(fail(NBG_ERR_UNSUPPORTED, "too many synapses"));
@@ -940,6 +1073,10 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(e->out_ptr.upload(optr), "out_ptr");
     chk(e->out_bit.upload(obit), "out_bit");
     chk(e->out_delay.upload(odelay), "out_delay");
+    chk(e->gen_ptr.upload(gptr), "gen_ptr");
+    chk(e->gen_pos.upload(gpos), "gen_pos");
+    chk(e->gen_src.upload(gsrc), "gen_src");
+    chk(e->gen_delay.upload(gdelay), "gen_delay");
     chk(e->blk_spk.alloc((size_t)kMaxBlockSteps * N), "block spike lists");
     chk(e->blk_cnt.alloc(kMaxBlockSteps), "block counts");
     chk(e->err.alloc(1), "err");
@@ -969,7 +1106,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     if (st != NBG_OK) return bail(st);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
-    e->prop_grid = std::max(1, sms) * 4;
+    e->prop_grid = std::max(1, sms) * 2;
     e->spike_capacity = opt.spike_capacity;
     *out = e;
     return NBG_OK;
@@ -1057,7 +1194,7 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
                 }
                 cudaGraph_t g;
                 NBG_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-                for (int k = 0; k < G; ++k) launch_block(e, nd, B, k);
+                for (int k = 0; k < G; ++k) launch_block(e, nd, B, k, true);
                 NBG_CUDA(cudaStreamEndCapture(e->stream, &g));
                 cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
                 cudaGraphDestroy(g);
@@ -1116,12 +1253,16 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     e->spk_t.resize(base + (size_t)nspk);
     if (nspk > 0)
         NBG_CUDA(cudaMemcpy(e->spk_id.data() + base, e->out_ids.p, nspk * sizeof(int), cudaMemcpyDeviceToHost));
-    size_t off = base;
+    size_t in = base, out = base;
     for (int k = 0; k < count; ++k) {
-        std::sort(e->spk_id.begin() + off, e->spk_id.begin() + off + cnt[k]);
-        std::fill(e->spk_t.begin() + off, e->spk_t.begin() + off + cnt[k], t0 + k);
-        off += cnt[k];
+        const size_t step_begin = out;
+        for (int q = 0; q < cnt[k]; ++q, ++in)
+            if (e->spk_id[in] >= 0) e->spk_id[out++] = e->spk_id[in];
+        std::sort(e->spk_id.begin() + step_begin, e->spk_id.begin() + out);
+        std::fill(e->spk_t.begin() + step_begin, e->spk_t.begin() + out, t0 + k);
     }
+    e->spk_id.resize(out);
+    e->spk_t.resize(out);
     if (ntr > 0) {
         const size_t rb = e->trace_rows.size();
         e->trace_rows.resize(rb + (size_t)count * ntr);
@@ -1277,6 +1418,8 @@ nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value) {
     if (!e) return fail(NBG_ERR_INVALID, "null engine");
     if (id < 0 || id >= e->N) return fail(NBG_ERR_INVALID, "neuron id %d out of range", id);
     if (t < e->next_t) return fail(NBG_ERR_INVALID, "time %d is in the past (next step %d)", t, e->next_t);
+    if (e->layers[e->pop_host[id]].generator)
+        return fail(NBG_ERR_UNSUPPORTED, "neuron %d belongs to a source-free PoissonRate layer (evaluated inline)", id);
     if (!std::isfinite(value)) return fail(NBG_ERR_INVALID, "current must be finite");
     nbg_engine::CurrentEvent c{t, id, value};
     auto it = std::upper_bound(e->currents.begin(), e->currents.end(), c,

@@ -331,7 +331,7 @@ class NetworkDescription:
         return int(self.layer_count.sum())
 
     def flat(self, dt: float, semantics: int = _lib.SEM_LEGACY_CPU, seed: int = 0) -> dict:
-        return {"layer_model": self.layer_model, "layer_count": self.layer_count,
+        return {"layer_model": self.layer_model, "layer_count": self.layer_count, "layer_output": self.layer_output,
                 "layer_fparams": self.layer_fparams, "layer_iparams": self.layer_iparams,
                 "source": self.source, "target": self.target, "type": self.type, "weight": self.weight,
                 "max_weight": self.max_weight, "delay": self.delay, "rule": self.rule,

@@ -36,6 +36,7 @@ def make_desc(flat: dict):
             layers[i].f[k] = float(flat["layer_fparams"][i][k])
         for k in range(_lib.NIP):
             layers[i].ip[k] = int(flat["layer_iparams"][i][k])
+        layers[i].output = int(bool(flat["layer_output"][i]))
     rp = flat["rule_params"]
     rules = (_lib.StdpDesc * max(1, len(rp)))()
     for r in range(len(rp)):

@@ -85,6 +85,13 @@ def _lib(prec: int):
             "num_logged_events": (ctypes.c_int64, [vp]),
             "get_events": (None, [vp, i32p, i64p, f64p]),
             "add_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+            "dense_create": (vp, [ctypes.c_int, ctypes.c_int, f32p, f32p, i32p, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float]),
+            "dense_destroy": (None, [vp]),
+            "dense_run": (ctypes.c_int, [vp, ctypes.c_int]),
+            "dense_num_steps": (ctypes.c_int64, [vp]),
+            "dense_counts": (None, [vp, i32p]),
+            "dense_state": (None, [vp, f64p, i32p, ctypes.POINTER(ctypes.c_uint8)]),
             "poisson_hash": (ctypes.c_float, [ctypes.c_int, ctypes.c_int]),
             "gauss12": (ctypes.c_double, [ctypes.c_uint64, ctypes.c_int, ctypes.c_int]),
         }
@@ -202,3 +209,47 @@ class OracleNet:
         if n:
             self._f("get_events")(self.h, _ptr(t, ctypes.c_int), _ptr(c, ctypes.c_int64), _ptr(w, ctypes.c_double))
         return t, c, w
+
+
+class OracleDense:
+    """B instances x N voltage-jump LIF neurons sharing a dense W (row = pre):
+    the semantics of the GPU dense delivery engine (include/nbg_dense.h)."""
+
+    def __init__(self, instances: int, neurons: int, w, fparams, iparams, drive_rate_hz: float,
+                 drive_weight: float, dt: float, precision: int = 32):
+        self.lib = _lib(precision)
+        self._f = lambda name: getattr(self.lib, f"orc{precision}_{name}")
+        self.B, self.N = int(instances), int(neurons)
+        self.w = np.ascontiguousarray(w, np.float32)
+        self.fp = np.ascontiguousarray(fparams, np.float32)
+        self.ip = np.ascontiguousarray(iparams, np.int32)
+        self.h = self._f("dense_create")(self.B, self.N, _ptr(self.w, ctypes.c_float), _ptr(self.fp, ctypes.c_float),
+                                         _ptr(self.ip, ctypes.c_int), float(drive_rate_hz), float(drive_weight),
+                                         float(dt))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self._f("dense_destroy")(h)
+            self.h = None
+
+    def run(self, steps: int) -> "OracleDense":
+        if self._f("dense_run")(self.h, int(steps)) != 0:
+            raise ValueError("steps must be positive")
+        return self
+
+    def counts(self) -> np.ndarray:
+        n = int(self._f("dense_num_steps")(self.h))
+        out = np.empty(n, np.int32)
+        if n:
+            self._f("dense_counts")(self.h, _ptr(out, ctypes.c_int))
+        return out
+
+    def state(self):
+        tot = self.B * self.N
+        v = np.empty(tot, np.float64)
+        last = np.empty(tot, np.int32)
+        s = np.empty(tot, np.uint8)
+        self._f("dense_state")(self.h, _ptr(v, ctypes.c_double), _ptr(last, ctypes.c_int),
+                               s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        return v, last, s

@@ -740,6 +740,134 @@ void ORC(add_current)(void *hp, int t, int id, double value) {
     n->cur_v[n->cur_t.n - 1] = (REAL)value;
 }
 
+/* ------------------------------------------------------------------------
+ * Dense all-to-all populations (the GPU dense delivery engine's semantics):
+ * B instances x N voltage-jump LIF neurons sharing W (N x N, row = pre).
+ * Step t: a = sum over spiking pre i (ascending) of W[i][j], plus the drive
+ * weight when the delay-1 PoissonRate source (hash index b*N+j) fired at t-1;
+ * if not refractory V += a; then the legacy Euler update
+ * (TimeDrivenLIF_Voltage_jump.cpp:49-86).  The first run performs N+1 updates.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int B, N, t_ref, next_t, ran;
+    REAL v_rest, tau, v_th, r, v_reset, i_ext, dt, drive_w;
+    float drive_p;
+    const float *w; /* borrowed: N x N */
+    REAL *v;
+    int *last;
+    unsigned char *s, *s_next;
+    vec64_t counts;
+} dense_t;
+
+void *ORC(dense_create)(int B, int N, const float *w, const float *f, const int *ip, float drive_rate_hz,
+                        float drive_w, float dt) {
+    dense_t *d = (dense_t *)calloc(1, sizeof(dense_t));
+    d->B = B;
+    d->N = N;
+    d->w = w;
+    d->v_rest = (REAL)f[0];
+    d->tau = (REAL)f[1];
+    d->v_th = (REAL)f[2];
+    d->r = (REAL)f[3];
+    d->v_reset = (REAL)f[4] + (REAL)f[5];
+    d->i_ext = (REAL)f[6];
+    d->t_ref = ip[0];
+    d->dt = (REAL)dt;
+    d->drive_w = (REAL)drive_w;
+    float rate = drive_rate_hz > 0.0f ? drive_rate_hz : 0.0f;
+    float p = rate * dt * 0.001f;
+    d->drive_p = p < 1.0f ? p : 1.0f;
+    size_t tot = (size_t)B * N;
+    d->v = (REAL *)malloc(tot * sizeof(REAL));
+    d->last = (int *)malloc(tot * sizeof(int));
+    d->s = (unsigned char *)calloc(tot, 1);
+    d->s_next = (unsigned char *)calloc(tot, 1);
+    for (size_t i = 0; i < tot; ++i) {
+        d->v[i] = d->v_reset;
+        d->last[i] = 10000;
+    }
+    return d;
+}
+
+void ORC(dense_destroy)(void *hp) {
+    dense_t *d = (dense_t *)hp;
+    if (!d) return;
+    free(d->v);
+    free(d->last);
+    free(d->s);
+    free(d->s_next);
+    free(d->counts.v);
+    free(d);
+}
+
+static void dense_step(dense_t *d, int t) {
+    const int N = d->N;
+    REAL *col = (REAL *)malloc((size_t)N * sizeof(REAL));
+    int64_t nspk = 0;
+    for (int b = 0; b < d->B; ++b) {
+        const unsigned char *sb = d->s + (size_t)b * N;
+        for (int j = 0; j < N; ++j) col[j] = K(0.0);
+        for (int i = 0; i < N; ++i) {
+            if (!sb[i]) continue;
+            const float *row = d->w + (size_t)i * N;
+            for (int j = 0; j < N; ++j) col[j] = col[j] + (REAL)row[j];
+        }
+        for (int j = 0; j < N; ++j) {
+            const size_t idx = (size_t)b * N + j;
+            REAL a = col[j];
+            if (t >= 1 && hash_uniform01((int)idx, t - 1) < d->drive_p) a = a + d->drive_w;
+            REAL vv = d->v[idx];
+            int ls = d->last[idx];
+            if (ls > d->t_ref) vv = vv + a;
+            REAL cur = K(0.0);
+            cur = cur + d->r * d->i_ext / d->tau;
+            REAL aux = (ls > d->t_ref) ? cur + (d->v_rest - vv) / d->tau : K(0.0);
+            vv = vv + aux * d->dt;
+            ls += 1;
+            unsigned char spk = 0;
+            if (vv > d->v_th) {
+                vv = d->v_reset;
+                ls = 0;
+                spk = 1;
+                ++nspk;
+            }
+            d->v[idx] = vv;
+            d->last[idx] = ls;
+            d->s_next[idx] = spk;
+        }
+    }
+    unsigned char *tmp = d->s;
+    d->s = d->s_next;
+    d->s_next = tmp;
+    vpush(&d->counts, nspk);
+    free(col);
+}
+
+int ORC(dense_run)(void *hp, int steps) {
+    dense_t *d = (dense_t *)hp;
+    if (steps <= 0) return 1;
+    int count = d->ran ? steps : steps + 1;
+    for (int k = 0; k < count; ++k) dense_step(d, d->next_t + k);
+    d->next_t += count;
+    d->ran = 1;
+    return 0;
+}
+
+int64_t ORC(dense_num_steps)(void *hp) { return ((dense_t *)hp)->counts.n; }
+void ORC(dense_counts)(void *hp, int *out) {
+    dense_t *d = (dense_t *)hp;
+    for (int64_t k = 0; k < d->counts.n; ++k) out[k] = (int)d->counts.v[k];
+}
+void ORC(dense_state)(void *hp, double *v, int *last, unsigned char *s) {
+    dense_t *d = (dense_t *)hp;
+    size_t tot = (size_t)d->B * d->N;
+    for (size_t i = 0; i < tot; ++i) {
+        if (v) v[i] = (double)d->v[i];
+        if (last) last[i] = d->last[i];
+        if (s) s[i] = d->s[i];
+    }
+}
+
 /* standalone helpers for known-answer tests */
 float ORC(poisson_hash)(int neuron_index, int time_step) { return hash_uniform01(neuron_index, time_step); }
 double ORC(gauss12)(uint64_t seed, int neuron, int t) { return (double)gauss12(seed, neuron, t); }

@@ -1,0 +1,105 @@
+"""Hand-written adjoint of the recurrent LIF network.
+
+GPU: gradients of the CUDA forward + adjoint (FP32) against
+  * FP64 torch autograd of the same discretised dynamics (reference_forward),
+    in sigmoid-smoothed mode and in spiking mode with the same fast-sigmoid
+    surrogate (relative tolerance 1e-4 of the largest gradient entry);
+  * central finite differences, eps = 1e-3, of the FP64 loss in smoothed mode
+    (relative tolerance 2e-3 per checked entry).
+CPU: torch.autograd.gradcheck of reference_forward itself in FP64.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from neuronbridge_gb300.adjoint import reference_forward
+
+KW = dict(n_in=16, n_rec=32, n_out=5, checkpoint=20, weight_scale=20.0, seed=11)
+T, B = 60, 4
+
+
+def _setup(smooth, device="cuda"):
+    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+
+    torch.manual_seed(0)
+    model = RecurrentLIF(smooth=smooth, device=device, **KW)
+    rates = torch.linspace(5.0, 50.0, KW["n_in"]) * 8.0
+    x = poisson_inputs(rates, T, B, dt=1.0, seed=3)
+    labels = torch.randint(0, KW["n_out"], (B,), generator=torch.Generator().manual_seed(6)).to(device)
+    return model, x, labels
+
+
+def _params(model):
+    return [model.w_in, model.w_rec, model.w_out, model.alpha, model.theta]
+
+
+def _ref_loss(model, x, labels, params, smooth):
+    y = reference_forward(x, *params, smooth=smooth, t_ref=model.params.t_ref, slope=model.params.slope)
+    return torch.nn.functional.cross_entropy(y, labels)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("smooth", [True, False])
+def test_adjoint_matches_fp64_autograd(smooth):
+    model, x, labels = _setup(smooth)
+    loss = torch.nn.functional.cross_entropy(model(x), labels)
+    loss.backward()
+    ours = [p.grad.detach().double().cpu() for p in _params(model)]
+    ref_params = [p.detach().double().cpu().requires_grad_(True) for p in _params(model)]
+    ref_loss = _ref_loss(model, x.double().cpu(), labels.cpu(), ref_params, smooth)
+    ref_loss.backward()
+    assert abs(loss.item() - ref_loss.item()) < 1e-4 * max(1.0, abs(ref_loss.item()))
+    for name, g, r in zip(("w_in", "w_rec", "w_out", "alpha", "theta"), ours, ref_params):
+        scale = r.grad.abs().max().item()
+        assert scale > 0, name
+        err = (g - r.grad).abs().max().item()
+        assert err <= 1e-4 * scale, (name, err, scale)
+
+
+@pytest.mark.gpu
+def test_adjoint_matches_central_differences_smoothed():
+    model, x, labels = _setup(True)
+    torch.nn.functional.cross_entropy(model(x), labels).backward()
+    xd, ld = x.double().cpu(), labels.cpu()
+    base = [p.detach().double().cpu() for p in _params(model)]
+    rng = np.random.default_rng(1)
+    eps = 1e-3
+    for pi, p in enumerate(_params(model)):
+        g = p.grad.detach().double().cpu().reshape(-1)
+        for idx in rng.choice(g.numel(), size=min(6, g.numel()), replace=False):
+            vals = []
+            for sgn in (1, -1):
+                ps = [b.clone() for b in base]
+                ps[pi].view(-1)[idx] += sgn * eps
+                vals.append(_ref_loss(model, xd, ld, ps, True).item())
+            fd = (vals[0] - vals[1]) / (2 * eps)
+            assert abs(fd - g[idx].item()) <= 2e-3 * max(abs(fd), 1e-3), (pi, int(idx), fd, g[idx].item())
+
+
+@pytest.mark.gpu
+def test_full_size_step_runs():
+    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+
+    model = RecurrentLIF()  # 256 -> 1024 -> 10, T = 1000, checkpoints every 100
+    rates = torch.empty(256).uniform_(5.0, 50.0, generator=torch.Generator().manual_seed(5))
+    x = poisson_inputs(rates, 1000, 128, dt=1.0, seed=5)
+    labels = torch.randint(0, 10, (128,), generator=torch.Generator().manual_seed(6)).cuda()
+    loss = torch.nn.functional.cross_entropy(model(x), labels)
+    loss.backward()
+    for p in _params(model):
+        assert torch.isfinite(p.grad).all()
+
+
+def test_reference_dynamics_gradcheck_cpu():
+    torch.manual_seed(0)
+    Tn, Bn, C, N, O = 8, 2, 3, 4, 2
+    x = (torch.rand(Tn, Bn, C, dtype=torch.float64) < 0.3).double()
+    params = [torch.randn(C, N, dtype=torch.float64) * 8, torch.randn(N, N, dtype=torch.float64) * 5,
+              torch.randn(N, O, dtype=torch.float64), torch.full((N,), 0.05, dtype=torch.float64),
+              torch.full((N,), -50.0, dtype=torch.float64)]
+    params = [p.requires_grad_(True) for p in params]
+    f = lambda *ps: reference_forward(x, *ps, smooth=True, slope=1.0)
+    assert torch.autograd.gradcheck(f, params, eps=1e-6, atol=1e-6, rtol=1e-4)
+    assert math.isfinite(f(*params).sum().item())
