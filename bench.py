@@ -2,6 +2,14 @@
 pair-STDP network (RK4, dt = 0.1 ms, 10M synapses).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload izh|lif|batched|dense|adjoint]
+
+The default workload is the headline (izh).  The others measure the remaining
+configurations with the same timing rules and print one JSON line each:
+lif (1,000 LIF + Poisson), batched (256 LIF instances in one engine vs one
+engine per instance), dense (64 x 8192 LIF, split-BF16 tensor-core delivery
+vs the FP32 CUDA-core path, error vs FP64), adjoint (recurrent LIF forward +
+hand-written adjoint, B=128, T=1000).
 
 One benchmark step = one run call of 10,000 simulation steps (1 s of
 simulated time) through the public API; the default K = 10 covers the
@@ -110,20 +118,22 @@ def _post_fanout(desc) -> np.ndarray:
     return np.bincount(desc.target[desc.rule >= 0], minlength=desc.neuron_count)
 
 
-def cpu_baseline_sample(sim_steps: int = 1500) -> dict:
+def cpu_baseline_sample(sim_steps: int = 3000) -> dict:
     """The oracle port on the same 100k/10M network for a bounded number of
-    simulation steps (single host thread)."""
+    simulation steps, OpenMP over all host cores (identical results to one
+    thread: each thread owns disjoint neurons and synapses)."""
     import oracle
     from neuronbridge_gb300 import workloads
 
+    cores = os.cpu_count() or 1
     net, cfg = workloads.izhikevich_stdp()
-    o = oracle.OracleNet(net.to_native().flat(cfg.timestep, seed=2))
+    o = oracle.OracleNet(net.to_native().flat(cfg.timestep, seed=2)).set_threads(cores)
     t0 = time.perf_counter()
     o.run(sim_steps)
     dt = time.perf_counter() - t0
-    return {"value": o.num_events / dt, "unit": "synaptic events/s", "cores": 1, "kind": "port",
+    return {"value": o.num_events / dt, "unit": "synaptic events/s", "cores": cores, "kind": "port",
             "sample": f"100k-neuron Izhikevich+STDP network, first {sim_steps + 1} simulation steps, "
-                      f"oracle FP32 restatement, 1 host thread",
+                      f"oracle FP32 restatement, OpenMP over {cores} host threads",
             "neuron_steps_per_s": 100_000 * (sim_steps + 1) / dt, "seconds": dt}
 
 
@@ -136,9 +146,10 @@ def run_reference(args) -> None:
     import oracle
     from neuronbridge_gb300 import workloads
 
+    cores = os.cpu_count() or 1
     net, cfg = workloads.izhikevich_stdp()
-    o = oracle.OracleNet(net.to_native().flat(cfg.timestep, seed=2))
-    sample = 300  # simulation steps per benchmark step: a bounded sample
+    o = oracle.OracleNet(net.to_native().flat(cfg.timestep, seed=2)).set_threads(cores)
+    sample = 1000  # simulation steps per benchmark step: a bounded sample
     for k in range(args.warmup + args.steps):
         e0 = o.num_events
         t0 = time.perf_counter()
@@ -155,13 +166,220 @@ def run_reference(args) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "izhikevich_stdp_100k", "neurons": 100_000, "synapses": 10_000_000,
                    "sim_steps_per_step": sample, "dt_ms": 0.1},
-        "cpu_baseline": {"value": value, "unit": "synaptic events/s", "cores": 1, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "synaptic events/s", "cores": cores, "kind": "port",
                          "sample": f"{sample} simulation steps per benchmark step of the 100k/10M network, "
                                    "oracle FP32 restatement (the reference's CPU path does not build here: "
-                                   "it needs Boost and its CMake build), 1 host thread"},
+                                   f"it needs Boost and its CMake build), OpenMP over {cores} host threads"},
         "e2e": {"value": value, "unit": "synaptic events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _common(args, metric, value, unit, ms_per_step, config, **extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config}
+    line.update(extra)
+    return line
+
+
+def bench_lif(args) -> dict:
+    """1,000 LIF + 1,000 Poisson: one benchmark step = one run(10,000) call."""
+    import torch
+
+    import neuronbridge_gb300 as nb
+    from neuronbridge_gb300 import workloads
+
+    net, cfg = workloads.plain_lif()
+    sim = nb.Simulation(net, cfg, kernel_timing=True)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        sim.run(cfg.steps)
+        sim.clear_spikes()
+        flush.fill_(1.0)
+    ev = dev = upd = 0.0
+    launches = 0
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.steps):
+        e0 = sim.num_events
+        sim.run(cfg.steps)
+        p = sim.bench_profiling_snapshot()
+        ev += sim.num_events - e0
+        dev += p["device_ms"] / 1e3
+        upd += p["update_kernel_ms"] / 1e3
+        launches += p["kernel_launches"]
+        sim.clear_spikes()
+        flush.fill_(1.0)
+    clk = clocks.stop()
+    n = 2000
+    upd_bytes = 24 * 1000 * cfg.steps * args.steps + 12 * ev
+    peak, kind = _peaks()
+    return _common(args, "synaptic events/s", ev / dev, "synaptic events/s", 1e3 * dev / args.steps,
+                   {"workload": "plain_lif_1k", "neurons": n, "sim_steps_per_step": cfg.steps,
+                    "block_steps": sim.block_steps},
+                   neuron_steps_per_s=n * cfg.steps * args.steps / dev,
+                   roofline={"bound": "hbm", "kernel": "k_update", "achieved": upd_bytes / upd / 1e9, "peak": peak,
+                             "unit": "GB/s", "frac": upd_bytes / upd / 1e9 / peak, "peak_kind": kind,
+                             "traffic": None},
+                   gpu_launches=int(launches), clocks=clk)
+
+
+def bench_batched(args) -> dict:
+    """256 LIF instances (500..50,000 neurons each): one engine over the
+    union, autotuned launch shape, one graph per run(1,000) call, against the
+    same 256 networks each in its own engine, run one after the other."""
+    import neuronbridge_gb300 as nb
+    from neuronbridge_gb300 import tuning, workloads
+
+    t0 = time.perf_counter()
+    singles, union, cfg = workloads.batched_lif()
+    build_s = time.perf_counter() - t0
+    sim = nb.Simulation(union, cfg, kernel_timing=True)
+    tune = tuning.autotune(sim, trial_steps=300)
+    for _ in range(args.warmup):
+        sim.run(cfg.steps)
+        sim.clear_spikes()
+    ev = dev = wall = 0.0
+    launches = 0
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.steps):
+        e0 = sim.num_events
+        w0 = time.perf_counter()
+        sim.run(cfg.steps)
+        wall += time.perf_counter() - w0
+        p = sim.bench_profiling_snapshot()
+        ev += sim.num_events - e0
+        dev += p["device_ms"] / 1e3
+        launches += p["kernel_launches"]
+        sim.clear_spikes()
+    clk = clocks.stop()
+    n_lif = union.neuron_count // 2
+    del sim
+    # plain form: every instance in its own engine, one after another
+    p_ev = p_dev = p_wall = 0.0
+    for net in singles:
+        s = nb.Simulation(net, cfg)
+        s.run(cfg.steps)  # warm (first call: steps + 1 updates)
+        e0 = s.num_events
+        w0 = time.perf_counter()
+        s.run(cfg.steps)
+        p_wall += time.perf_counter() - w0
+        p_ev += s.num_events - e0
+        p_dev += s.bench_profiling_snapshot()["device_ms"] / 1e3
+        s.close()
+    value = ev / dev
+    plain = p_ev / p_dev
+    return _common(args, "synaptic events/s", value, "synaptic events/s", 1e3 * dev / args.steps,
+                   {"workload": "batched_lif_256", "instances": 256, "lif_neurons": n_lif,
+                    "sim_steps_per_step": cfg.steps, "tuned": tune["choice"], "host_build_s": build_s},
+                   neuron_steps_per_s=n_lif * cfg.steps * args.steps / dev,
+                   plain={"value": plain, "unit": "synaptic events/s", "device_s_per_1000_steps": p_dev,
+                          "wall_s_per_1000_steps": p_wall},
+                   speedup_vs_plain=value / plain,
+                   e2e={"value": ev / wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
+                        "d2h_bytes_per_step": None},
+                   gpu_launches=int(launches), clocks=clk)
+
+
+def bench_dense(args) -> dict:
+    """64 instances x 8,192 LIF sharing W (N(0, 1/8192)); one benchmark step =
+    run(500).  Split-BF16 tensor-core delivery vs the FP32 CUDA-core path, and
+    the delivery error of both against FP64 S W on the spike matrices of the
+    run (sampled every benchmark step)."""
+    import torch
+
+    from neuronbridge_gb300 import NeuronLayer
+    from neuronbridge_gb300.dense import DensePopulations, dense_weights
+    from neuronbridge_gb300.workloads import LIF_PARAMS
+
+    n, per = 8192, 500
+    w = dense_weights(n)
+    layer = NeuronLayer("TimeDrivenLIF_Voltage_jump", 1, parameters=dict(LIF_PARAMS))
+    w64 = torch.from_numpy(w).double().cuda()
+    out = {}
+    for prec in ("split_bf16", "fp32"):
+        eng = DensePopulations(w, layer, precision=prec)
+        for _ in range(args.warmup):
+            eng.run(per)
+        dev = dl = 0.0
+        errs = []
+        clocks = ClockSampler(0)
+        clocks.start()
+        for _ in range(args.steps):
+            eng.run(per)
+            p = eng.profile()
+            dev += p["device_ms"] / 1e3
+            dl += p["delivery_ms"] / 1e3
+            s = eng.spikes()
+            got = eng.deliver(s)
+            ref = (torch.from_numpy(s).double().cuda() @ w64).cpu().numpy()
+            errs.append(float(np.abs(got - ref).max()))
+        clk = clocks.stop()
+        out[prec] = {"ms_per_step": 1e3 * dev / (args.steps * per), "delivery_us": 1e6 * dl / (args.steps * per),
+                     "max_abs_err_vs_fp64": max(errs), "clocks": clk,
+                     "spikes_per_step": float(eng.spike_counts()[-per:].mean())}
+        del eng
+    sp = out["split_bf16"]
+    byts = 2 * 2 * n * n + 64 * n * 2 + 2 * 64 * n * 4
+    flops = 2 * 64 * n * n * 2
+    peak, kind = _peaks()
+    achieved = byts / (sp["delivery_us"] * 1e-6) / 1e9
+    return _common(args, "steps/s", 1e3 / sp["ms_per_step"], "steps/s", sp["ms_per_step"] * per,
+                   {"workload": "dense_split_bf16_64x8192", "instances": 64, "neurons": n, "sim_steps_per_step": per},
+                   neuron_steps_per_s=64 * n * 1e3 / sp["ms_per_step"],
+                   roofline={"bound": "hbm", "kernel": "k_dense_gemm (split BF16, mma.sync)", "achieved": achieved,
+                             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind,
+                             "traffic": None, "tflops": flops / (sp["delivery_us"] * 1e-6) / 1e12},
+                   paths=out)
+
+
+def bench_adjoint(args) -> dict:
+    """Recurrent LIF (256 -> 1024 -> 10, B = 128, T = 1000): forward alone,
+    and forward + hand-written adjoint backward, per training step."""
+    import torch
+
+    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+
+    model = RecurrentLIF()
+    rates = torch.empty(256).uniform_(5.0, 50.0, generator=torch.Generator().manual_seed(5))
+    x = poisson_inputs(rates, 1000, 128, dt=1.0, seed=5)
+    labels = torch.randint(0, 10, (128,), generator=torch.Generator().manual_seed(6)).cuda()
+    lossf = torch.nn.functional.cross_entropy
+
+    def fwd():
+        with torch.no_grad():
+            return lossf(model(x), labels)
+
+    def step():
+        model.zero_grad(set_to_none=True)
+        loss = lossf(model(x), labels)
+        loss.backward()
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        fwd()
+    e1.record()
+    torch.cuda.synchronize()
+    f_ms = e0.elapsed_time(e1) / args.steps
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    t_ms = e0.elapsed_time(e1) / args.steps
+    gflop = 2 * 128 * (256 * 1024 + 1024 * 1024 + 1024 * 10) * 1000 / 1e9
+    return _common(args, "training steps/s", 1e3 / t_ms, "steps/s", t_ms,
+                   {"workload": "adjoint_rlif_b128_t1000", "batch": 128, "T": 1000, "n_rec": 1024,
+                    "checkpoint": 100},
+                   forward_ms=f_ms, backward_ms=t_ms - f_ms, backward_over_forward=(t_ms - f_ms) / f_ms,
+                   forward_tflops=gflop / f_ms)
 
 
 def main() -> None:
@@ -172,11 +390,16 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sim-steps", type=int, default=SIM_STEPS_PER_BENCH_STEP)
+    ap.add_argument("--workload", default="izh", choices=["izh", "lif", "batched", "dense", "adjoint"])
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "izh":
+        fn = {"lif": bench_lif, "batched": bench_batched, "dense": bench_dense, "adjoint": bench_adjoint}
+        print(json.dumps(fn[args.workload](args)), flush=True)
         return
 
     world, rank, local = _dist()

@@ -146,6 +146,10 @@ nbg_status nbg_num_neurons(const nbg_engine *e, int *n);
 nbg_status nbg_num_synapses(const nbg_engine *e, int64_t *s);
 /* minimum delay over synapses (the temporal-blocking window) */
 nbg_status nbg_block_steps(const nbg_engine *e, int *b);
+/* Change the launch shape of a live engine: threads per block (multiple of
+ * 32, <= 256) and steps per update launch (1 .. min delay; 0 = the min
+ * delay).  Results do not depend on either; only speed does. */
+nbg_status nbg_set_launch(nbg_engine *e, int threads_per_block, int block_steps);
 
 /* State fields for nbg_get_state / nbg_set_state. */
 enum {

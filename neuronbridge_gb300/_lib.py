@@ -84,6 +84,7 @@ _SIGNATURES = {
     "nbg_num_neurons": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "nbg_num_synapses": (ctypes.c_int, [ctypes.c_void_p, _i64p]),
     "nbg_block_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "nbg_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "nbg_get_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _f32p]),
     "nbg_set_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _f32p]),
     "nbg_num_spikes": (ctypes.c_int, [ctypes.c_void_p, _i64p]),

@@ -106,6 +106,8 @@ struct NetDev {
     int dtab_len;
     const float *rule_a; // [rule][2] = max_ltp, max_ltd
     unsigned int *mask;
+    unsigned int *wsum; // per slot: one bit per mask word, set while that word is non-zero
+    int Ws;             // summary words per slot (ceil(Wt / 32) + 1 padding word)
     const int *out_ptr;
     const unsigned int *out_bit;
     const unsigned short *out_delay;
@@ -392,7 +394,32 @@ __device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts) 
 //     (every mark for the block's slots was made by earlier launches);
 //   * the post-synaptic STDP pass of a spiking neuron is spread over its warp:
 //     the 32 lanes stride over that neuron's CSC list.
-constexpr int kPrefetch = 4;
+// Bits [woff, woff+nw) of a summary row (nw <= 32), as an nw-bit mask.
+__device__ __forceinline__ unsigned int summary_bits(const unsigned int *srow, int woff, int nw) {
+    const int w0 = woff >> 5, sh = woff & 31;
+    unsigned long long x = srow[w0];
+    if (sh + nw > 32) x |= (unsigned long long)srow[w0 + 1] << 32;
+    x >>= sh;
+    return nw >= 32 ? (unsigned int)x : (unsigned int)x & ((1u << nw) - 1u);
+}
+
+// Clear `bits` (relative to woff) in a summary row; neighbours share words.
+__device__ __forceinline__ void summary_clear(unsigned int *srow, int woff, unsigned int bits) {
+    const int w0 = woff >> 5, sh = woff & 31;
+    const unsigned long long x = (unsigned long long)bits << sh;
+    if ((unsigned int)x) atomicAnd(&srow[w0], ~(unsigned int)x);
+    if (x >> 32) atomicAnd(&srow[w0 + 1], ~(unsigned int)(x >> 32));
+}
+
+// Clear the summary bits of words [woff, woff+nw) for any nw.
+__device__ __forceinline__ void summary_clear_range(unsigned int *srow, int woff, int nw) {
+    for (int w = woff; w < woff + nw;) {
+        const int take = min(32 - (w & 31), woff + nw - w);
+        const unsigned int m = take == 32 ? 0xffffffffu : ((1u << take) - 1u) << (w & 31);
+        if (srow[w >> 5] & m) atomicAnd(&srow[w >> 5], ~m);
+        w += take;
+    }
+}
 
 __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -428,54 +455,73 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
 #pragma unroll 4
         for (int b = 0; b < B; ++b) nz[b] = L.p[5] * gauss12(n.seed, j, T0 + b);
     }
-    const int npre = nw < kPrefetch ? nw : kPrefetch;
-    unsigned int nxt[kPrefetch] = {0u, 0u, 0u, 0u};
-    if (active) {
-        const unsigned int *row0 = n.mask + (size_t)((unsigned int)T0 % (unsigned int)n.D) * n.Wt + woff;
-#pragma unroll
-        for (int k = 0; k < kPrefetch; ++k)
-            if (k < npre) nxt[k] = row0[k];
-    }
+    // Fast path (in-degree <= 1024, <= 32 generator inputs): the L2-resident
+    // word summary says which of this neuron's mask words hold arrivals, so
+    // only those words are loaded from HBM; the summary of step b+1 is
+    // fetched while step b runs.  Otherwise every word is scanned.
+    const bool fast = nw <= 32 && (g1 - g0) <= 32;
+    unsigned int snext = 0u;
+    if (active && fast && nw > 0)
+        snext = summary_bits(n.wsum + (size_t)((unsigned int)T0 % (unsigned int)n.D) * n.Ws, woff, nw);
     unsigned long long delivered = 0;
     for (int b = 0; b < B; ++b) {
         const int t = T0 + b;
         bool spk = false;
         if (active) {
-            unsigned int cur[kPrefetch];
-#pragma unroll
-            for (int k = 0; k < kPrefetch; ++k) cur[k] = nxt[k];
-            unsigned int *mrow = n.mask + (size_t)((unsigned int)t % (unsigned int)n.D) * n.Wt + woff;
-            if (b + 1 < B) {
-                const unsigned int *mnext = n.mask + (size_t)((unsigned int)(t + 1) % (unsigned int)n.D) * n.Wt + woff;
-#pragma unroll
-                for (int k = 0; k < kPrefetch; ++k)
-                    if (k < npre) nxt[k] = mnext[k];
-            }
+            const unsigned int slot = (unsigned int)t % (unsigned int)n.D;
+            unsigned int *mrow = n.mask + (size_t)slot * n.Wt + woff;
             float acc_a = 0.0f, acc_b = 0.0f;
             const bool gate = r.last > L.ip;
-            int gq = g0;
-            for (int wi = 0; wi < nw; ++wi) {
-                unsigned int word;
-                if (wi < kPrefetch) {
-                    word = cur[0];
-#pragma unroll
-                    for (int k = 1; k < kPrefetch; ++k)
-                        if (wi == k) word = cur[k];
-                } else {
-                    word = mrow[wi];
+            if (fast) {
+                const unsigned int sb = snext;
+                if (b + 1 < B && nw > 0)
+                    snext = summary_bits(n.wsum + (size_t)((unsigned int)(t + 1) % (unsigned int)n.D) * n.Ws, woff, nw);
+                // generator arrivals of this step (pure functions of source and time)
+                unsigned int gfired = 0u, gwords = 0u;
+                for (int g = g0; g < g1; ++g)
+                    if (generator_fired(n, n.gen_src[g], t - (int)n.gen_delay[g])) {
+                        gfired |= 1u << (g - g0);
+                        gwords |= 1u << (n.gen_pos[g] >> 5);
+                    }
+                unsigned int need = sb | gwords;
+                if (sb) summary_clear(n.wsum + (size_t)slot * n.Ws, woff, sb);
+                while (need) {
+                    const int wi = __ffs(need) - 1;
+                    need &= need - 1u;
+                    unsigned int word = 0u;
+                    if ((sb >> wi) & 1u) {
+                        word = mrow[wi];
+                        mrow[wi] = 0u;
+                    }
+                    for (unsigned int gf = gfired; gf; gf &= gf - 1u) {
+                        const int gp = n.gen_pos[g0 + __ffs(gf) - 1];
+                        if ((gp >> 5) == wi) word |= 1u << (gp & 31);
+                    }
+                    delivered += __popc(word);
+                    while (word) {
+                        const int p = wi * 32 + __ffs(word) - 1;
+                        word &= word - 1u;
+                        apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
+                    }
                 }
-                if (word) mrow[wi] = 0u;
-                // generator arrivals of this word, evaluated inline
-                for (; gq < g1 && (n.gen_pos[gq] >> 5) == wi; ++gq)
-                    if (generator_fired(n, n.gen_src[gq], t - (int)n.gen_delay[gq]))
-                        word |= 1u << (n.gen_pos[gq] & 31);
-                if (!word) continue;
-                delivered += __popc(word);
-                while (word) {
-                    const int p = wi * 32 + __ffs(word) - 1;
-                    word &= word - 1u;
-                    apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
+            } else {
+                int gq = g0;
+                for (int wi = 0; wi < nw; ++wi) {
+                    unsigned int word = mrow[wi];
+                    if (word) mrow[wi] = 0u;
+                    for (; gq < g1 && (n.gen_pos[gq] >> 5) == wi; ++gq)
+                        if (generator_fired(n, n.gen_src[gq], t - (int)n.gen_delay[gq]))
+                            word |= 1u << (n.gen_pos[gq] & 31);
+                    if (!word) continue;
+                    delivered += __popc(word);
+                    while (word) {
+                        const int p = wi * 32 + __ffs(word) - 1;
+                        word &= word - 1u;
+                        apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
+                    }
                 }
+                // this neuron's summary bits (set while its words were non-zero)
+                summary_clear_range(n.wsum + (size_t)slot * n.Ws, woff, nw);
             }
             spk = update_neuron(n, L, r, acc_a, acc_b, nz[b], j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
@@ -518,7 +564,7 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
 // Propagate the spikes of the last B steps: one warp per spike, lanes over its
 // out-synapses; also appends the spikes to the run's raster in step order and
 // advances the device clock.  The last CTA to finish publishes the cursor.
-__global__ void __launch_bounds__(256) k_propagate(NetDev n, int B) {
+__global__ void __launch_bounds__(256, 2) k_propagate(NetDev n, int B) {
     __shared__ int pre[kMaxBlockSteps + 1];
     const int T0 = *n.tnow;
     const int run_t0 = *n.run_t0;
@@ -550,7 +596,9 @@ __global__ void __launch_bounds__(256) k_propagate(NetDev n, int B) {
         for (int q = q0 + lane; q < q1; q += 32) {
             const unsigned int bit = n.out_bit[q];
             const unsigned int slot = (t + n.out_delay[q]) % (unsigned int)n.D;
-            atomicOr(&n.mask[(size_t)slot * n.Wt + (bit >> 5)], 1u << (bit & 31u));
+            const unsigned int wd = bit >> 5;
+            const unsigned int old = atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
+            if (old == 0u) atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
         }
     }
     if (blockIdx.x == 0 && (int)threadIdx.x < B) n.out_cnt[T0 - run_t0 + threadIdx.x] = n.blk_cnt[threadIdx.x];
@@ -580,6 +628,7 @@ struct nbg_engine {
     int D = 1, Wt = 0, dmin = 1, dmax = 1, B = 1;
     int threads = 256;
     int n_rules = 0;
+    bool plastic = false; // any synapse with a learning rule
     float dt = 1.0f;
     int semantics = 0;
     unsigned long long seed = 0;
@@ -604,7 +653,8 @@ struct nbg_engine {
     DevBuf<unsigned short> gen_delay;
     DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, blk_spk, blk_cnt, out_ids, out_cnt, err, tnow, run_t0,
         trace_slot, ev_t, ev_pos;
-    DevBuf<unsigned int> mask, out_bit, done;
+    DevBuf<unsigned int> mask, wsum, out_bit, done;
+    int Ws = 1;
     DevBuf<unsigned short> out_delay;
     DevBuf<long long> cursor;
     DevBuf<unsigned long long> ev_cursor, n_events;
@@ -629,7 +679,7 @@ struct nbg_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph = nullptr;
-    int graph_blocks = 0, graph_B = 0;
+    int graph_blocks = 0, graph_tail = 0, graph_B = 0, graph_threads = 0;
     NetDev graph_nd{}; // kernel arguments baked into the graph
     int prop_grid = 0;
     double last_ms = 0.0, last_upd_ms = 0.0, last_prop_ms = 0.0;
@@ -667,6 +717,8 @@ struct nbg_engine {
         n.dtab_len = dtab_len;
         n.rule_a = rule_a.p;
         n.mask = mask.p;
+        n.wsum = wsum.p;
+        n.Ws = Ws;
         n.out_ptr = out_ptr.p;
         n.out_bit = out_bit.p;
         n.out_delay = out_delay.p;
@@ -749,11 +801,14 @@ nbg_status reset_state(nbg_engine *e) {
     NBG_CUDA(cudaMemcpy(e->last.p, last0.data(), e->N * sizeof(int), cudaMemcpyHostToDevice));
     if (e->S > 0) {
         NBG_CUDA(cudaMemcpy(e->w.p, e->init_w.data(), e->S * sizeof(float), cudaMemcpyHostToDevice));
-        NBG_CUDA(e->apre.zero());
-        NBG_CUDA(e->apost.zero());
-        NBG_CUDA(e->slast.zero());
+        if (e->plastic) {
+            NBG_CUDA(e->apre.zero());
+            NBG_CUDA(e->apost.zero());
+            NBG_CUDA(e->slast.zero());
+        }
     }
     NBG_CUDA(e->mask.zero());
+    NBG_CUDA(e->wsum.zero());
     NBG_CUDA(e->blk_cnt.zero());
     NBG_CUDA(e->err.zero());
     NBG_CUDA(e->tnow.zero());
@@ -774,7 +829,18 @@ nbg_status reset_state(nbg_engine *e) {
     return NBG_OK;
 }
 
-constexpr int kGraphBlocks = 64;
+constexpr int kLaunchChunk = 64; // direct launches between timing harvests
+
+// Grow the pool of event triples used to bracket the launches.
+nbg_status ensure_timing_events(nbg_engine *e, int blocks) {
+    if (!e->kernel_timing) return NBG_OK;
+    while ((int)e->tev.size() < 3 * blocks) {
+        cudaEvent_t ev;
+        NBG_CUDA(cudaEventCreate(&ev));
+        e->tev.push_back(ev);
+    }
+    return NBG_OK;
+}
 
 // Launch one block of B steps.  With kernel timing, `slot` selects the event
 // triple bracketing the two kernels.
@@ -997,6 +1063,8 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
         src_of[p] = d->source[s];
     }
     e->init_w = w;
+    e->plastic = false;
+    for (int64_t s = 0; s < S && !e->plastic; ++s) e->plastic = d->rule[s] >= 0;
 
     // ---- CSR by source over (mask bit, delay); generator sources excluded
     std::vector<int> optr((size_t)e->N + 1, 0);
@@ -1049,10 +1117,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
     chk(cudaEventCreate(&e->ev0), "event");
     chk(cudaEventCreate(&e->ev1), "event");
-    if (e->kernel_timing) {
-        e->tev.resize(3 * kGraphBlocks, nullptr);
-        for (auto &ev : e->tev) chk(cudaEventCreate(&ev), "timing event");
-    }
+
     chk(e->pop.upload(pop), "pop");
     chk(e->meta.upload(meta), "meta");
     const size_t N = (size_t)e->N;
@@ -1065,11 +1130,15 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(e->csc_ptr_d.upload(cptr), "csc_ptr");
     chk(e->woff.upload(woff), "woff");
     chk(e->w.alloc((size_t)S), "w");
-    chk(e->wmax.upload(wmax), "wmax");
-    chk(e->apre.alloc((size_t)S), "apre");
-    chk(e->apost.alloc((size_t)S), "apost");
-    chk(e->slast.alloc((size_t)S), "slast");
+    if (e->plastic) { // STDP state and weight bounds only when some synapse learns
+        chk(e->wmax.upload(wmax), "wmax");
+        chk(e->apre.alloc((size_t)S), "apre");
+        chk(e->apost.alloc((size_t)S), "apost");
+        chk(e->slast.alloc((size_t)S), "slast");
+    }
     chk(e->mask.alloc((size_t)e->D * e->Wt), "mask ring");
+    e->Ws = (e->Wt + 31) / 32 + 1;
+    chk(e->wsum.alloc((size_t)e->D * e->Ws), "mask summary ring");
     chk(e->out_ptr.upload(optr), "out_ptr");
     chk(e->out_bit.upload(obit), "out_bit");
     chk(e->out_delay.upload(odelay), "out_delay");
@@ -1170,63 +1239,67 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         }
         e->currents.swap(later);
     }
-    int t = t0;
-    size_t ci = 0;
     const int t_end = t0 + count;
-    while (t < t_end) {
-        while (ci < due.size() && due[ci].t == t) {
-            NBG_CUDA(cudaMemcpyAsync(e->iext.p + due[ci].id, &due[ci].value, sizeof(float), cudaMemcpyHostToDevice,
-                                     e->stream));
-            NBG_CUDA(cudaStreamSynchronize(e->stream)); // the host value is a stack copy
-            ++ci;
+    if (e->use_graph && due.empty()) {
+        // the whole call as one graph: nfull blocks of B steps and a tail block
+        const int nfull = count / B, tail = count % B;
+        const int nblocks = nfull + (tail ? 1 : 0);
+        nbg_status ps = ensure_timing_events(e, nblocks);
+        if (ps != NBG_OK) return ps;
+        if (!e->graph || e->graph_blocks != nfull || e->graph_tail != tail || e->graph_B != B ||
+            e->graph_threads != e->threads || std::memcmp(&e->graph_nd, &nd, sizeof(NetDev)) != 0) {
+            if (e->graph) {
+                cudaGraphExecDestroy(e->graph);
+                e->graph = nullptr;
+            }
+            cudaGraph_t g;
+            NBG_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < nfull; ++k) launch_block(e, nd, B, k, true);
+            if (tail) launch_block(e, nd, tail, nfull, true);
+            NBG_CUDA(cudaStreamEndCapture(e->stream, &g));
+            cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) return fail(NBG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+            e->graph_blocks = nfull;
+            e->graph_tail = tail;
+            e->graph_B = B;
+            e->graph_threads = e->threads;
+            e->graph_nd = nd;
         }
-        const int seg_end = ci < due.size() ? due[ci].t : t_end;
-        const int seg = seg_end - t;
-        const int nfull = seg / B, tail = seg % B;
-        int done_blocks = 0;
-        if (e->use_graph && nfull >= 8) {
-            const int G = std::min(nfull, kGraphBlocks);
-            if (!e->graph || e->graph_blocks != G || e->graph_B != B ||
-                std::memcmp(&e->graph_nd, &nd, sizeof(NetDev)) != 0) {
-                if (e->graph) {
-                    cudaGraphExecDestroy(e->graph);
-                    e->graph = nullptr;
+        NBG_CUDA(cudaGraphLaunch(e->graph, e->stream));
+        nbg_status hs = harvest_timing(e, nblocks);
+        if (hs != NBG_OK) return hs;
+        launches += 2LL * nblocks;
+    } else {
+        // direct launches, split at timed current injections
+        nbg_status ps = ensure_timing_events(e, kLaunchChunk);
+        if (ps != NBG_OK) return ps;
+        int t = t0;
+        size_t ci = 0;
+        while (t < t_end) {
+            while (ci < due.size() && due[ci].t == t) {
+                NBG_CUDA(cudaMemcpyAsync(e->iext.p + due[ci].id, &due[ci].value, sizeof(float),
+                                         cudaMemcpyHostToDevice, e->stream));
+                NBG_CUDA(cudaStreamSynchronize(e->stream)); // the host value is a vector element
+                ++ci;
+            }
+            const int seg_end = ci < due.size() ? due[ci].t : t_end;
+            const int seg = seg_end - t;
+            const int nblocks = (seg + B - 1) / B;
+            int slot = 0;
+            for (int k = 0; k < nblocks; ++k) {
+                launch_block(e, nd, std::min(B, seg - k * B), slot++);
+                launches += 2;
+                if (slot == kLaunchChunk) {
+                    nbg_status hs = harvest_timing(e, slot);
+                    if (hs != NBG_OK) return hs;
+                    slot = 0;
                 }
-                cudaGraph_t g;
-                NBG_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-                for (int k = 0; k < G; ++k) launch_block(e, nd, B, k, true);
-                NBG_CUDA(cudaStreamEndCapture(e->stream, &g));
-                cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
-                cudaGraphDestroy(g);
-                if (ie != cudaSuccess) return fail(NBG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
-                e->graph_blocks = G;
-                e->graph_B = B;
-                e->graph_nd = nd;
             }
-            const int reps = nfull / G;
-            for (int k = 0; k < reps; ++k) {
-                NBG_CUDA(cudaGraphLaunch(e->graph, e->stream));
-                nbg_status hs = harvest_timing(e, G); // event triples are reused by the next replay
-                if (hs != NBG_OK) return hs;
-            }
-            done_blocks = reps * G;
-            launches += (int64_t)reps * G * 2;
-        }
-        int slot = 0;
-        for (int k = done_blocks; k < nfull + (tail ? 1 : 0); ++k) {
-            launch_block(e, nd, k < nfull ? B : tail, slot++);
-            launches += 2;
-            if (slot == kGraphBlocks) {
-                nbg_status hs = harvest_timing(e, slot);
-                if (hs != NBG_OK) return hs;
-                slot = 0;
-            }
-        }
-        {
             nbg_status hs = harvest_timing(e, slot);
             if (hs != NBG_OK) return hs;
+            t = seg_end;
         }
-        t = seg_end;
     }
     NBG_CUDA(cudaGetLastError());
     NBG_CUDA(cudaEventRecord(e->ev1, e->stream));
@@ -1311,6 +1384,21 @@ nbg_status nbg_block_steps(const nbg_engine *e, int *b) {
     return NBG_OK;
 }
 
+nbg_status nbg_set_launch(nbg_engine *e, int threads_per_block, int block_steps) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (threads_per_block <= 0 || threads_per_block % 32 || threads_per_block > 256)
+        return fail(NBG_ERR_INVALID, "threads_per_block must be a multiple of 32 and <= 256");
+    if (block_steps < 0) return fail(NBG_ERR_INVALID, "block_steps must be >= 0");
+    const int B = block_steps > 0 ? std::min(block_steps, e->dmin) : e->dmin;
+    e->threads = threads_per_block;
+    e->B = std::max(1, std::min(B, kMaxBlockSteps));
+    if (e->graph) {
+        cudaGraphExecDestroy(e->graph);
+        e->graph = nullptr;
+    }
+    return NBG_OK;
+}
+
 nbg_status nbg_get_state(nbg_engine *e, int field, float *out) {
     if (!e || !out) return fail(NBG_ERR_INVALID, "null argument");
     NBG_CUDA(cudaSetDevice(e->device));
@@ -1391,10 +1479,16 @@ nbg_status nbg_get_weights(nbg_engine *e, float *w, float *apre, float *apost, i
     float *srcs[3] = {e->w.p, e->apre.p, e->apost.p};
     for (int k = 0; k < 3; ++k) {
         if (!dst[k]) continue;
+        if (!srcs[k]) { // no plastic synapse: traces are identically zero
+            for (size_t p = 0; p < S; ++p) dst[k][p] = 0.0f;
+            continue;
+        }
         NBG_CUDA(cudaMemcpy(tmp.data(), srcs[k], S * sizeof(float), cudaMemcpyDeviceToHost));
         for (size_t p = 0; p < S; ++p) dst[k][e->csc_orig[p]] = tmp[p];
     }
-    if (last) {
+    if (last && !e->plastic) {
+        for (size_t p = 0; p < S; ++p) last[p] = 0;
+    } else if (last) {
         itmp.resize(S);
         NBG_CUDA(cudaMemcpy(itmp.data(), e->slast.p, S * sizeof(int), cudaMemcpyDeviceToHost));
         for (size_t p = 0; p < S; ++p) last[e->csc_orig[p]] = itmp[p];

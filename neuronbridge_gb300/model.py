@@ -326,6 +326,29 @@ class NetworkDescription:
         self.rule_params = (np.stack([r.native_params() for r in rules]) if rules
                             else np.zeros((0, 4), np.float32))
 
+    @classmethod
+    def from_arrays(cls, layers: list[NeuronLayer], source, target, synapse_type, weight, max_weight=None,
+                    delay=1, synapse_rule=-1, rules: list[LearningRule] | None = None) -> "NetworkDescription":
+        """Build directly from flat connection arrays (original connection
+        order = array order), without Connection objects."""
+        d = cls(layers, [], rules or [])
+        n = len(source)
+
+        def arr(x, dt):
+            a = np.asarray(x, dtype=dt)
+            return np.full(n, a, dtype=dt) if a.ndim == 0 else np.ascontiguousarray(a.ravel())
+
+        d.source = arr(source, np.int32)
+        d.target = arr(target, np.int32)
+        d.type = arr(synapse_type, np.int32)
+        d.weight = arr(weight, np.float32)
+        d.max_weight = d.weight.copy() if max_weight is None else arr(max_weight, np.float32)
+        d.delay = arr(delay, np.int32)
+        d.rule = arr(synapse_rule, np.int32)
+        if not (len(d.target) == len(d.type) == len(d.weight) == len(d.delay) == len(d.rule) == n):
+            raise ValueError("connection arrays must have one entry per connection")
+        return d
+
     @property
     def neuron_count(self) -> int:
         return int(self.layer_count.sum())

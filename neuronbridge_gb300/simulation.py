@@ -159,6 +159,11 @@ class Simulation:
         _lib.check(self.lib.nbg_block_steps(self._h, ctypes.byref(b)))
         return b.value
 
+    def set_launch(self, threads_per_block: int = 256, block_steps: int = 0) -> "Simulation":
+        """Change the launch shape (speed only; results are independent of it)."""
+        _lib.check(self.lib.nbg_set_launch(self._h, int(threads_per_block), int(block_steps)))
+        return self
+
     def state_field(self, field: int) -> np.ndarray:
         out = np.empty(self.description.neuron_count, np.float32)
         _lib.check(self.lib.nbg_get_state(self._h, int(field), _p(out, ctypes.c_float)))

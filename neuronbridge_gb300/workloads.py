@@ -28,7 +28,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .model import Connection, LearningRule, Network, NeuronLayer, SimulationConfig, float32, int32
+from .model import (Connection, LearningRule, Network, NetworkDescription, NeuronLayer, SimulationConfig, float32,
+                    int32)
 
 LIF_PARAMS = {"V_rest": float32(-65.0), "V_reset": float32(-65.0), "V_th": float32(-50.0), "tau": float32(20.0),
               "R": float32(1.0), "t_ref": int32(20)}
@@ -98,59 +99,81 @@ def batched_sizes(instances: int = 256, lo: int = 500, hi: int = 50_000, seed: i
 
 def lif_instance_arrays(n: int, seed: int, in_degree: float = 100.0) -> tuple[np.ndarray, np.ndarray]:
     """Seeded Erdos-Renyi recurrent connectivity of one batched-LIF instance
-    (local ids): the number of synapses is Binomial(n(n-1), p) with
-    p = in_degree/(n-1); pairs are drawn uniformly without autapses and
-    duplicates are dropped."""
+    (local ids, no autapses, no multapses) with p = in_degree/(n-1): a dense
+    Bernoulli mask for n <= 4096, else Binomial(n(n-1), p) uniform pairs with
+    duplicates dropped."""
     rng = np.random.default_rng(seed)
     p = min(1.0, in_degree / max(1, n - 1))
+    if n <= 4096:
+        mask = rng.random((n, n)) < p
+        np.fill_diagonal(mask, False)
+        src, tgt = np.nonzero(mask)
+        return src.astype(np.int32), tgt.astype(np.int32)
     m = int(rng.binomial(n * (n - 1), p))
     src = rng.integers(0, n, size=m, dtype=np.int64)
     tgt = rng.integers(0, n - 1, size=m, dtype=np.int64)
     tgt = tgt + (tgt >= src)
-    key = np.unique(src * n + tgt)
+    key = src * n + tgt
+    key.sort()
+    key = key[np.concatenate(([True], key[1:] != key[:-1]))]  # drop multapses
     return (key // n).astype(np.int32), (key % n).astype(np.int32)
 
 
-def lif_instance(n: int, src: np.ndarray, tgt: np.ndarray, rate_hz: float, delay: int = 15,
-                 offset: int = 0) -> tuple[list[NeuronLayer], list[Connection]]:
-    """Layers and connections of one batched-LIF instance with neuron ids
-    starting at ``offset``: a LIF layer of n, then its Poisson layer of n."""
+def _instance_layers(n: int, rate_hz: float) -> list[NeuronLayer]:
+    return [_lif_layer(n), NeuronLayer.poisson_rate(n, rate_bias_hz=rate_hz, rate_gain_hz_per_current=0.0)]
+
+
+def _instance_arrays(n: int, seed: int, offset: int = 0, delay: int = 15):
+    """(source, target, type, weight, delay) of one instance, ids from offset:
+    recurrent E (+0.5) / I (type 1, 2.5) synapses, then the 1:1 Poisson drive."""
+    src, tgt = lif_instance_arrays(n, seed)
     n_exc = (n * 4) // 5
-    exc = src < n_exc
-    conns = [
-        Connection(src[exc] + offset, tgt[exc] + offset, synapse_type=0, weight=0.5, delay=delay),
-        Connection(src[~exc] + offset, tgt[~exc] + offset, synapse_type=1, weight=2.5, delay=delay),
-    ]
-    ids = np.arange(n, dtype=np.int32) + offset
-    conns.append(Connection(ids + n, ids, synapse_type=0, weight=0.5, delay=1))
-    layers = [_lif_layer(n), NeuronLayer.poisson_rate(n, rate_bias_hz=rate_hz, rate_gain_hz_per_current=0.0)]
-    return layers, conns
+    inh = src >= n_exc
+    ids = np.arange(n, dtype=np.int32)
+    s = np.concatenate([src, ids + n]) + offset
+    t = np.concatenate([tgt, ids]) + offset
+    ty = np.concatenate([inh.astype(np.int32), np.zeros(n, np.int32)])
+    w = np.concatenate([np.where(inh, 2.5, 0.5).astype(np.float32), np.full(n, 0.5, np.float32)])
+    d = np.concatenate([np.full(len(src), delay, np.int32), np.ones(n, np.int32)])
+    return s.astype(np.int32), t.astype(np.int32), ty, w, d
 
 
-def batched_lif(instances: int = 256, lo: int = 500, hi: int = 50_000, steps: int = 1000, seed: int = 3
-                ) -> tuple[list[Network], Network, SimulationConfig]:
-    """Configuration 2: returns (per-instance networks, the batched union, config).
-    Instance k uses connectivity seed 1000+k and a Poisson rate drawn
-    uniformly in [4, 12] kHz; the PoissonRate hash index stays local to each
-    instance's Poisson layer, as in the reference."""
+def batched_params(instances: int = 256, lo: int = 500, hi: int = 50_000, seed: int = 3):
+    """Instance sizes (log-uniform) and Poisson drive rates (uniform 4-12 kHz)."""
     sizes = batched_sizes(instances, lo, hi, seed)
     rates = np.random.default_rng(seed + 1).uniform(4000.0, 12000.0, size=instances)
-    singles, union = [], Network()
+    return sizes, rates
+
+
+def batched_instance(k: int, instances: int = 256, lo: int = 500, hi: int = 50_000, seed: int = 3
+                     ) -> NetworkDescription:
+    """Instance k alone: a LIF layer and its Poisson layer, connectivity seed
+    1000 + k.  The PoissonRate hash index stays local to the instance's
+    Poisson layer, as in the reference."""
+    sizes, rates = batched_params(instances, lo, hi, seed)
+    n = int(sizes[k])
+    s, t, ty, w, d = _instance_arrays(n, 1000 + k)
+    return NetworkDescription.from_arrays(_instance_layers(n, float(rates[k])), s, t, ty, w, delay=d)
+
+
+def batched_union(instances: int = 256, lo: int = 500, hi: int = 50_000, seed: int = 3) -> NetworkDescription:
+    """All instances as one network of disjoint blocks (instance k at an id
+    offset), the form the batched engine runs in one launch per block."""
+    sizes, rates = batched_params(instances, lo, hi, seed)
+    layers, parts = [], []
     offset = 0
     for k, n in enumerate(sizes):
         n = int(n)
-        src, tgt = lif_instance_arrays(n, 1000 + k)
-        single = Network()
-        layers, conns = lif_instance(n, src, tgt, float(rates[k]))
-        for l in layers:
-            single.add_layer(l)
-        for c in conns:
-            single.connect(c)
-        singles.append(single)
-        u_layers, u_conns = lif_instance(n, src, tgt, float(rates[k]), offset=offset)
-        for l in u_layers:
-            union.add_layer(l)
-        for c in u_conns:
-            union.connect(c)
+        layers += _instance_layers(n, float(rates[k]))
+        parts.append(_instance_arrays(n, 1000 + k, offset))
         offset += 2 * n
-    return singles, union, SimulationConfig(steps=steps, timestep=0.1)
+    cat = [np.concatenate([p[i] for p in parts]) for i in range(5)]
+    return NetworkDescription.from_arrays(layers, cat[0], cat[1], cat[2], cat[3], delay=cat[4])
+
+
+def batched_lif(instances: int = 256, lo: int = 500, hi: int = 50_000, steps: int = 1000, seed: int = 3
+                ) -> tuple[list[NetworkDescription], NetworkDescription, SimulationConfig]:
+    """Configuration 2 at small scale (tests): (per-instance descriptions, the
+    batched union, config)."""
+    singles = [batched_instance(k, instances, lo, hi, seed) for k in range(instances)]
+    return singles, batched_union(instances, lo, hi, seed), SimulationConfig(steps=steps, timestep=0.1)

@@ -46,7 +46,7 @@ def build(force: bool = False) -> None:
         out = _lib_path(prec)
         if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(_SRC):
             continue
-        cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+        cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
                *defs, _SRC, "-o", out + ".tmp", "-lm"]
         jobs.append((subprocess.Popen(cmd), out))
     for proc, out in jobs:
@@ -84,6 +84,7 @@ def _lib(prec: int):
             "set_event_log": (None, [vp, ctypes.c_int]),
             "num_logged_events": (ctypes.c_int64, [vp]),
             "get_events": (None, [vp, i32p, i64p, f64p]),
+            "set_threads": (None, [vp, ctypes.c_int]),
             "add_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             "dense_create": (vp, [ctypes.c_int, ctypes.c_int, f32p, f32p, i32p, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float]),
@@ -193,6 +194,11 @@ class OracleNet:
         if n:
             self._f("get_traces")(self.h, _ptr(out, ctypes.c_double))
         return out.reshape(-1, self._ntrace)
+
+    def set_threads(self, threads: int) -> "OracleNet":
+        """OpenMP threads for the per-step loops (results do not change)."""
+        self._f("set_threads")(self.h, int(threads))
+        return self
 
     def add_current(self, t: int, neuron: int, value: float) -> None:
         """Set neuron's external current to ``value`` at the start of step t."""

@@ -33,6 +33,9 @@
  * (L/Network/src/Network.cu:485-502).
  */
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -117,6 +120,10 @@ typedef struct {
     vec64_t cur_t, cur_id;
     REAL *cur_v;
     int64_t cur_vcap;
+    int threads;          /* OpenMP threads for the per-step loops (1 = serial) */
+    unsigned char *fired; /* per-neuron spike flags of the current update */
+    int64_t *seg;         /* target segment starts of the sorted bucket */
+    int64_t seg_cap;
 } net_t;
 
 static void vpush(vec64_t *a, int64_t x) {
@@ -299,6 +306,8 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
     n->i_ext = (REAL *)calloc(nn, sizeof(REAL));
     n->rate = (REAL *)calloc(nn, sizeof(REAL));
     n->last = (int *)malloc(nn * sizeof(int));
+    n->fired = (unsigned char *)calloc(nn, 1);
+    n->threads = 1;
     for (int l = 0; l < n_layers; ++l) {
         layer_t *L = &n->layers[l];
         for (int i = L->start; i < L->start + L->count; ++i) {
@@ -384,6 +393,8 @@ void ORC(destroy)(void *hp) {
     free(n->cur_t.v);
     free(n->cur_id.v);
     free(n->cur_v);
+    free(n->fired);
+    free(n->seg);
     free(n);
 }
 
@@ -444,7 +455,6 @@ static void deliver(net_t *n, int64_t p, int t) {
         }
         n->ev_w[n->ev_t.n - 1] = w;
     }
-    n->n_events++;
     switch (L->model) {
     case M_LIF_VJ:
         /* TimeDrivenLIF_Voltage_jump::ProcessSpike (.cpp:100-113): gated by
@@ -597,33 +607,60 @@ static int spiked_poisson(net_t *n, layer_t *L, int i, int t) {
     return s;
 }
 
+static int spiked(net_t *n, layer_t *L, int i, int t) {
+    switch (L->model) {
+    case M_LIF_VJ: return spiked_lif(n, L, i);
+    case M_IZH_COND: return spiked_izh_cond(n, L, i);
+    case M_IZH_RK4: return spiked_izh_rk4(n, L, i, t);
+    default: return spiked_poisson(n, L, i, t);
+    }
+}
+
+/* One step.  With threads > 1 the arrivals of different targets, the neuron
+ * updates and the post-synaptic passes of different spiking neurons run in
+ * parallel; each touches only its own neuron and synapses, so the results
+ * are identical to the serial order. */
 static void step(net_t *n, int t) {
     for (int64_t k = 0; k < n->cur_t.n; ++k)
         if (n->cur_t.v[k] == t) n->i_ext[n->cur_id.v[k]] = n->cur_v[k];
     /* 1. arrivals due at t, per target in CSC order */
     vec64_t *b = &n->bucket[t % n->ring];
     qsort(b->v, (size_t)b->n, sizeof(int64_t), cmp_i64);
-    for (int64_t e = 0; e < b->n; ++e) deliver(n, b->v[e], t);
+    n->n_events += b->n;
+    if (n->threads <= 1 || n->log_events || b->n < 4096) {
+        for (int64_t e = 0; e < b->n; ++e) deliver(n, b->v[e], t);
+    } else {
+        if (b->n + 1 > n->seg_cap) {
+            n->seg_cap = 2 * (b->n + 1);
+            n->seg = (int64_t *)realloc(n->seg, (size_t)n->seg_cap * sizeof(int64_t));
+        }
+        int64_t ns = 0;
+        for (int64_t e = 0; e < b->n; ++e)
+            if (e == 0 || n->csc_tgt[b->v[e]] != n->csc_tgt[b->v[e - 1]]) n->seg[ns++] = e;
+        n->seg[ns] = b->n;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(n->threads)
+        for (int64_t g = 0; g < ns; ++g)
+            for (int64_t e = n->seg[g]; e < n->seg[g + 1]; ++e) deliver(n, b->v[e], t);
+    }
     b->n = 0;
     /* 2. model updates in layer creation order */
     for (int l = 0; l < n->n_layers; ++l) {
         layer_t *L = &n->layers[l];
-        for (int i = L->start; i < L->start + L->count; ++i) {
-            int s = 0;
-            switch (L->model) {
-            case M_LIF_VJ: s = spiked_lif(n, L, i); break;
-            case M_IZH_COND: s = spiked_izh_cond(n, L, i); break;
-            case M_IZH_RK4: s = spiked_izh_rk4(n, L, i, t); break;
-            case M_POISSON: s = spiked_poisson(n, L, i, t); break;
-            }
-            if (!s) continue;
+        const int i0 = L->start, i1 = L->start + L->count;
+#pragma omp parallel for schedule(static) num_threads(n->threads) if (n->threads > 1 && L->count >= 4096)
+        for (int i = i0; i < i1; ++i) n->fired[i] = (unsigned char)spiked(n, L, i, t);
+        int64_t first = n->spk.n;
+        for (int i = i0; i < i1; ++i) {
+            if (!n->fired[i]) continue;
             vpush(&n->spk, ((int64_t)t << 32) | (int64_t)(uint32_t)i);
             for (int64_t q = n->out_ptr[i]; q < n->out_ptr[i + 1]; ++q) {
                 int64_t p = n->out_pos[q];
                 vpush(&n->bucket[(t + n->csc_delay[p]) % n->ring], p);
             }
-            stdp_post(n, i, t);
         }
+        const int64_t last = n->spk.n;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(n->threads) if (n->threads > 1 && last - first > 8)
+        for (int64_t k = first; k < last; ++k) stdp_post(n, (int)(n->spk.v[k] & 0xFFFFFFFF), t);
     }
     if (n->n_trace > 0) {
         if (n->trace_n + n->n_trace > n->trace_cap) {
@@ -633,6 +670,8 @@ static void step(net_t *n, int t) {
         for (int k = 0; k < n->n_trace; ++k) n->trace[n->trace_n++] = n->v[n->trace_ids[k]];
     }
 }
+
+void ORC(set_threads)(void *hp, int threads) { ((net_t *)hp)->threads = threads > 0 ? threads : 1; }
 
 /* Simulation::RunSimulationStep(steps) as seen through _core.Simulation.run:
  * N+1 updates on the first call, N afterwards. */
