@@ -54,6 +54,36 @@ nbg_status nbg_dense_deliver(nbg_dense *d, const uint8_t *s, float *out);
  * alone (CUDA events on the engine stream) */
 nbg_status nbg_dense_profile(nbg_dense *d, double *total_ms, double *delivery_ms, int64_t *launches);
 
+/* One split-BF16 spike delivery that allocates nothing -- no counterpart in
+ * the reference.
+ *
+ * For callers that cannot call cudaMalloc: a host that owns all device memory
+ * and hands the library its own buffers, a real-time control loop (the
+ * reference's closed-loop robot mode) where an allocator call may stall the
+ * device mid-run, or code whose stream is being captured in the global
+ * capture mode, where cudaMalloc is refused.  The caller passes every input
+ * and output as device pointers; the split-K partial sums live in a file-scope
+ * __device__ array of NBG_DENSE_NOALLOC_MAX_NEURONS * 64 * 2 floats (4 MiB),
+ * which every GPU that loads the library holds until the process exits.
+ *
+ *   w_hi_t, w_lo_t  BF16, neurons x neurons, row = post-synaptic neuron, column
+ *                   = pre-synaptic neuron (W transposed): W_hi = bf16(W),
+ *                   W_lo = bf16(W - W_hi), both round-to-nearest-even
+ *   spikes          BF16 0/1, 64 x neurons (instance-major)
+ *   out             FP32, 64 x neurons: out = spikes W
+ *   neurons         a multiple of 128, at most NBG_DENSE_NOALLOC_MAX_NEURONS
+ *                   (larger sizes are rejected with NBG_ERR_INVALID)
+ *
+ * The first call on a device looks up the scratch array's device address
+ * there (with that device current); make that first call before any stream
+ * capture.  Every call shares the one scratch array, so calls that overlap on
+ * the GPU (different streams, or different host threads on the same device)
+ * race: order them on one stream.  The scratch needs no clearing -- each call
+ * writes every partial sum it reads. */
+#define NBG_DENSE_NOALLOC_MAX_NEURONS 8192
+nbg_status nbg_dense_deliver_noalloc(const void *w_hi_t, const void *w_lo_t, const void *spikes, float *out,
+                                     int neurons, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "nbg_common.cuh"
@@ -554,3 +555,59 @@ nbg_status nbg_dense_profile(nbg_dense *d, double *total_ms, double *delivery_ms
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Delivery without allocation (nbg_dense_deliver_noalloc): the split-K
+// partial sums go to a file-scope device array instead of a buffer the
+// library allocates.  Host code must not use `g_noalloc_partial` as a device
+// address: it is a host-side stand-in for the symbol.  The real address is
+// looked up once per device with cudaGetSymbolAddress.
+
+static __device__ __align__(256) float g_noalloc_partial[kSplitK * kInstances * NBG_DENSE_NOALLOC_MAX_NEURONS];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float *g_noalloc_scratch[kNoAllocMaxDevices] = {};
+
+// out = partial[0] + partial[1]: the same fixed order as the update kernel
+__global__ void k_sum_split_partials(const float *__restrict__ part, float *__restrict__ out, int total) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) out[idx] = part[idx] + part[(size_t)total + idx];
+}
+
+} // namespace
+
+extern "C" nbg_status nbg_dense_deliver_noalloc(const void *w_hi_t, const void *w_lo_t, const void *spikes,
+                                                float *out, int neurons, void *stream) {
+    if (!w_hi_t || !w_lo_t || !spikes || !out) return nbg_fail(NBG_ERR_INVALID, "null argument");
+    if (neurons <= 0 || neurons % kBM != 0 || (neurons / kSplitK) % kBK != 0)
+        return nbg_fail(NBG_ERR_INVALID, "neurons must be a positive multiple of %d", kBM);
+    if (neurons > NBG_DENSE_NOALLOC_MAX_NEURONS)
+        return nbg_fail(NBG_ERR_INVALID, "neurons = %d exceeds the no-allocation limit of %d", neurons,
+                        NBG_DENSE_NOALLOC_MAX_NEURONS);
+    int dev = 0;
+    NBG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return nbg_fail(NBG_ERR_UNSUPPORTED, "device ordinal %d too large", dev);
+    float *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_scratch[dev]) { // first call on this device: set-up, with `dev` current
+            void *p = nullptr;
+            NBG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_partial));
+            NBG_CUDA(cudaFuncSetAttribute(k_dense_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
+            g_noalloc_scratch[dev] = static_cast<float *>(p);
+        }
+        scratch = g_noalloc_scratch[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    dim3 grid(neurons / kBM, kSplitK);
+    k_dense_gemm<<<grid, kGemmThreads, kGemmSmem, st>>>(static_cast<const __nv_bfloat16 *>(w_hi_t),
+                                                         static_cast<const __nv_bfloat16 *>(w_lo_t),
+                                                         static_cast<const __nv_bfloat16 *>(spikes), scratch, neurons);
+    const int total = kInstances * neurons;
+    k_sum_split_partials<<<(total + 255) / 256, 256, 0, st>>>(scratch, out, total);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
