@@ -294,7 +294,7 @@ def bench_dense(args) -> dict:
     from neuronbridge_gb300.dense import DensePopulations, dense_weights
     from neuronbridge_gb300.workloads import LIF_PARAMS
 
-    n, per = 8192, 500
+    n, per = 8192, (args.per or 500)
     w = dense_weights(n)
     layer = NeuronLayer("TimeDrivenLIF_Voltage_jump", 1, parameters=dict(LIF_PARAMS))
     w64 = torch.from_numpy(w).double().cuda()
@@ -391,6 +391,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sim-steps", type=int, default=SIM_STEPS_PER_BENCH_STEP)
     ap.add_argument("--workload", default="izh", choices=["izh", "lif", "batched", "dense", "adjoint"])
+    ap.add_argument("--per", type=int, default=None, help="simulation steps per benchmark step (dense)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

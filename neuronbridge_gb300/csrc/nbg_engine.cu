@@ -213,71 +213,155 @@ __device__ __forceinline__ float clamp_w(float w, float wmax) {
     return w;
 }
 
-// Pair STDP on synapse s at step t (L/LearningRule/src/Rule/STDP.cpp:19-61,
-// State/STDP_State.cpp:17-26): decay both traces from the host table by the
-// integer step gap, then the pre (Apre += 1, w -= A- Apost) or post
-// (Apost += 1, w += A+ Apre) jump and the clamp to [0, wmax].  All loads of
-// the synapse are independent and issued together.
-template <bool kPre>
-__device__ __forceinline__ void stdp_update(const NetDev &n, int s, int rule, int t, float w) {
-    const int last = n.slast[s];
-    const float apre = n.apre[s], apost = n.apost[s], wmax = n.wmax[s];
-    const float a = __ldg(&n.rule_a[rule * 2 + (kPre ? 1 : 0)]);
-    const int k = t - last;
-    float fp = 0.0f, fm = 0.0f;
-    if (k < n.dtab_len) {
-        fp = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + k]);
-        fm = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + k]);
+// Pair STDP (L/LearningRule/src/Rule/STDP.cpp:19-61, State/STDP_State.cpp:
+// 17-26): decay both traces from the host table by the integer step gap, then
+// the pre (Apre += 1, w -= A- Apost) or post (Apost += 1, w += A+ Apre) jump
+// and the clamp to [0, wmax].  Up to K synapses of one step with their loads
+// batched: the
+// state loads of all K are issued together, then the decay-table loads, so a
+// batch costs two memory round trips instead of two per synapse.  Entries
+// with meta < 2 (no rule) are skipped.  Same arithmetic as stdp_update.
+template <bool kPre, int K>
+__device__ __forceinline__ void stdp_batch(const NetDev &n, const int (&s)[K], const unsigned char (&meta)[K],
+                                           const float (&w0)[K], int t) {
+    int last[K];
+    float apre[K], apost[K], wmax[K], fp[K], fm[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (meta[k] >= 2) {
+            last[k] = n.slast[s[k]];
+            apre[k] = n.apre[s[k]];
+            apost[k] = n.apost[s[k]];
+            wmax[k] = n.wmax[s[k]];
+        }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        fp[k] = 0.0f;
+        fm[k] = 0.0f;
+        if (meta[k] >= 2) {
+            const int rule = (int)(meta[k] >> 1) - 1;
+            const int gap = t - last[k];
+            if (gap < n.dtab_len) {
+                fp[k] = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + gap]);
+                fm[k] = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + gap]);
+            }
+        }
     }
-    float xpre = apre * fp, xpost = apost * fm;
-    if (kPre) {
-        xpre = xpre + 1.0f;
-        w = clamp_w(w + (-a * xpost), wmax);
-    } else {
-        xpost = xpost + 1.0f;
-        w = clamp_w(w + a * xpre, wmax);
-    }
-    n.apre[s] = xpre;
-    n.apost[s] = xpost;
-    n.slast[s] = t;
-    n.w[s] = w;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (meta[k] >= 2) {
+            const int rule = (int)(meta[k] >> 1) - 1;
+            const float a = __ldg(&n.rule_a[rule * 2 + (kPre ? 1 : 0)]);
+            float xpre = apre[k] * fp[k], xpost = apost[k] * fm[k], w = w0[k];
+            if (kPre) {
+                xpre = xpre + 1.0f;
+                w = clamp_w(w + (-a * xpost), wmax[k]);
+            } else {
+                xpost = xpost + 1.0f;
+                w = clamp_w(w + a * xpre, wmax[k]);
+            }
+            n.apre[s[k]] = xpre;
+            n.apost[s[k]] = xpost;
+            n.slast[s[k]] = t;
+            n.w[s[k]] = w;
+        }
 }
 
-// Apply one arrival (ProcessSpike of the target model), then the pre hook.
-__device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
-                                              float &acc_b, bool gate, int s, int t) {
-    const unsigned char meta = n.meta[s];
-    const float w = n.w[s];
-    const int type = meta & 1;
-    const int rule = (int)(meta >> 1) - 1;
-    switch (M.model) {
-    case NBG_MODEL_LIF_VJ:
-        if (n.semantics == NBG_SEM_DENSE) {
-            if (type == 0) acc_a = acc_a + w;
-            else acc_b = acc_b + w;
-        } else if (gate) {
-            r.v = r.v + (type ? -w : w);
-        }
-        break;
-    case NBG_MODEL_IZH_COND:
-        if (type == 0) r.gexc = r.gexc + w;
-        else r.ginh = r.ginh + w;
-        break;
-    default: // IZH_RK4 current pulse, POISSON rate increment
-        acc_a = acc_a + (type ? -w : w);
-        break;
-    }
-    if (n.ev_t) {
-        unsigned long long pos = atomicAdd(n.ev_cursor, 1ull);
-        if (pos < (unsigned long long)n.ev_cap) {
-            n.ev_t[pos] = t;
-            n.ev_pos[pos] = s;
-            n.ev_w[pos] = w;
-        } else {
-            atomicOr(n.err, kErrEventLog);
+// Arrivals of one target are applied one at a time (a wider batch raises the
+// update kernel's register count past its occupancy target); the rarer
+// post-synaptic pass batches kPostChunk synapses per lane.
+constexpr int kArrivalChunk = 1;
+constexpr int kPostChunk = 2;
+
+// This lane's share of a post-synaptic STDP pass over in-synapses
+// [s, s1) of a spiking neuron, striding by the warp size.
+__device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t);
+
+// Apply c <= kArrivalChunk arrivals s[0..c) of one target, in order: the
+// target's ProcessSpike with the weight as it is before this step's pre
+// hook, then the pre hooks of the plastic ones.  Synapse loads are batched.
+__device__ __forceinline__ void apply_arrivals(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                               float &acc_b, bool gate, const int (&s)[kArrivalChunk], int c,
+                                               int t) {
+    unsigned char meta[kArrivalChunk];
+    float w[kArrivalChunk];
+#pragma unroll
+    for (int k = 0; k < kArrivalChunk; ++k) {
+        meta[k] = 0;
+        w[k] = 0.0f;
+        if (k < c) {
+            meta[k] = n.meta[s[k]];
+            w[k] = n.w[s[k]];
         }
     }
-    if (rule >= 0) stdp_update<true>(n, s, rule, t, w);
+#pragma unroll
+    for (int k = 0; k < kArrivalChunk; ++k) {
+        if (k >= c) break;
+        const int type = meta[k] & 1;
+        switch (M.model) {
+        case NBG_MODEL_LIF_VJ:
+            if (n.semantics == NBG_SEM_DENSE) {
+                if (type == 0) acc_a = acc_a + w[k];
+                else acc_b = acc_b + w[k];
+            } else if (gate) {
+                r.v = r.v + (type ? -w[k] : w[k]);
+            }
+            break;
+        case NBG_MODEL_IZH_COND:
+            if (type == 0) r.gexc = r.gexc + w[k];
+            else r.ginh = r.ginh + w[k];
+            break;
+        default: // IZH_RK4 current pulse, POISSON rate increment
+            acc_a = acc_a + (type ? -w[k] : w[k]);
+            break;
+        }
+        if (n.ev_t) {
+            const unsigned long long pos = atomicAdd(n.ev_cursor, 1ull);
+            if (pos < (unsigned long long)n.ev_cap) {
+                n.ev_t[pos] = t;
+                n.ev_pos[pos] = s[k];
+                n.ev_w[pos] = w[k];
+            } else {
+                atomicOr(n.err, kErrEventLog);
+            }
+        }
+    }
+    stdp_batch<true, kArrivalChunk>(n, s, meta, w, t);
+}
+
+// Apply every set bit of `word` (word index wi of this target) in ascending
+// order.
+__device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                           float &acc_b, bool gate, unsigned int word, int first, int t) {
+    while (word) {
+        int sp[kArrivalChunk];
+        int c = 0;
+#pragma unroll
+        for (int k = 0; k < kArrivalChunk; ++k) {
+            sp[k] = first;
+            if (word) {
+                sp[k] = first + __ffs(word) - 1;
+                word &= word - 1u;
+                c = k + 1;
+            }
+        }
+        apply_arrivals(n, M, r, acc_a, acc_b, gate, sp, c, t);
+    }
+}
+
+__device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t) {
+    for (; s < s1; s += 32 * kPostChunk) {
+        int ss[kPostChunk];
+        unsigned char mt[kPostChunk];
+        float w0[kPostChunk];
+#pragma unroll
+        for (int k = 0; k < kPostChunk; ++k) {
+            ss[k] = s + 32 * k;
+            mt[k] = ss[k] < s1 ? n.meta[ss[k]] : 0;
+            w0[k] = mt[k] >= 2 ? n.w[ss[k]] : 0.0f;
+        }
+        stdp_batch<false, kPostChunk>(n, ss, mt, w0, t);
+    }
 }
 
 // One neuron update; returns true on a spike.  `noise` is
@@ -394,6 +478,8 @@ __device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts) 
 //     (every mark for the block's slots was made by earlier launches);
 //   * the post-synaptic STDP pass of a spiking neuron is spread over its warp:
 //     the 32 lanes stride over that neuron's CSC list.
+constexpr int kPrefetch = 4; // mask words per neuron prefetched one step ahead
+
 // Bits [woff, woff+nw) of a summary row (nw <= 32), as an nw-bit mask.
 __device__ __forceinline__ unsigned int summary_bits(const unsigned int *srow, int woff, int nw) {
     const int w0 = woff >> 5, sh = woff & 31;
@@ -421,7 +507,7 @@ __device__ __forceinline__ void summary_clear_range(unsigned int *srow, int woff
     }
 }
 
-__global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
+__global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = j < n.N;
     const int lane = threadIdx.x & 31;
@@ -457,25 +543,46 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
     }
     // Fast path (in-degree <= 1024, <= 32 generator inputs): the L2-resident
     // word summary says which of this neuron's mask words hold arrivals, so
-    // only those words are loaded from HBM; the summary of step b+1 is
-    // fetched while step b runs.  Otherwise every word is scanned.
+    // only those words are loaded from HBM.  Two-stage prefetch: the summary
+    // bits of step b+2 and the flagged first kPrefetch mask words of step b+1
+    // are requested while step b runs (every mark for the block's slots was
+    // made by earlier launches, so both are final).
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
-    unsigned int snext = 0u;
-    if (active && fast && nw > 0)
-        snext = summary_bits(n.wsum + (size_t)((unsigned int)T0 % (unsigned int)n.D) * n.Ws, woff, nw);
+    const unsigned int D = (unsigned int)n.D;
+    unsigned int sb_cur = 0u, sb_nxt = 0u;
+    unsigned int w_cur[kPrefetch] = {0u, 0u, 0u, 0u};
+    if (active && fast && nw > 0) {
+        sb_cur = summary_bits(n.wsum + (size_t)((unsigned int)T0 % D) * n.Ws, woff, nw);
+        if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)((unsigned int)(T0 + 1) % D) * n.Ws, woff, nw);
+        const unsigned int *r0 = n.mask + (size_t)((unsigned int)T0 % D) * n.Wt + woff;
+#pragma unroll
+        for (int k = 0; k < kPrefetch; ++k)
+            if ((sb_cur >> k) & 1u) w_cur[k] = r0[k];
+    }
     unsigned long long delivered = 0;
     for (int b = 0; b < B; ++b) {
         const int t = T0 + b;
         bool spk = false;
         if (active) {
-            const unsigned int slot = (unsigned int)t % (unsigned int)n.D;
+            const unsigned int slot = (unsigned int)t % D;
             unsigned int *mrow = n.mask + (size_t)slot * n.Wt + woff;
             float acc_a = 0.0f, acc_b = 0.0f;
             const bool gate = r.last > L.ip;
             if (fast) {
-                const unsigned int sb = snext;
-                if (b + 1 < B && nw > 0)
-                    snext = summary_bits(n.wsum + (size_t)((unsigned int)(t + 1) % (unsigned int)n.D) * n.Ws, woff, nw);
+                const unsigned int sb = sb_cur;
+                unsigned int wc[kPrefetch];
+#pragma unroll
+                for (int k = 0; k < kPrefetch; ++k) wc[k] = w_cur[k];
+                // prefetch: flagged words of step b+1, summary of step b+2
+                if (b + 1 < B) {
+                    const unsigned int *rn = n.mask + (size_t)((unsigned int)(t + 1) % D) * n.Wt + woff;
+#pragma unroll
+                    for (int k = 0; k < kPrefetch; ++k) w_cur[k] = ((sb_nxt >> k) & 1u) ? rn[k] : 0u;
+                    sb_cur = sb_nxt;
+                    sb_nxt = (b + 2 < B && nw > 0)
+                                 ? summary_bits(n.wsum + (size_t)((unsigned int)(t + 2) % D) * n.Ws, woff, nw)
+                                 : 0u;
+                }
                 // generator arrivals of this step (pure functions of source and time)
                 unsigned int gfired = 0u, gwords = 0u;
                 for (int g = g0; g < g1; ++g)
@@ -490,7 +597,14 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
                     need &= need - 1u;
                     unsigned int word = 0u;
                     if ((sb >> wi) & 1u) {
-                        word = mrow[wi];
+                        if (wi < kPrefetch) {
+                            word = wc[0];
+#pragma unroll
+                            for (int k = 1; k < kPrefetch; ++k)
+                                if (wi == k) word = wc[k];
+                        } else {
+                            word = mrow[wi];
+                        }
                         mrow[wi] = 0u;
                     }
                     for (unsigned int gf = gfired; gf; gf &= gf - 1u) {
@@ -498,11 +612,7 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
                         if ((gp >> 5) == wi) word |= 1u << (gp & 31);
                     }
                     delivered += __popc(word);
-                    while (word) {
-                        const int p = wi * 32 + __ffs(word) - 1;
-                        word &= word - 1u;
-                        apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
-                    }
+                    apply_word(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
                 }
             } else {
                 int gq = g0;
@@ -514,11 +624,7 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
                             word |= 1u << (n.gen_pos[gq] & 31);
                     if (!word) continue;
                     delivered += __popc(word);
-                    while (word) {
-                        const int p = wi * 32 + __ffs(word) - 1;
-                        word &= word - 1u;
-                        apply_arrival(n, L, r, acc_a, acc_b, gate, base + p, t);
-                    }
+                    apply_word(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
                 }
                 // this neuron's summary bits (set while its words were non-zero)
                 summary_clear_range(n.wsum + (size_t)slot * n.Ws, woff, nw);
@@ -541,11 +647,7 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
             const int l = __ffs(sbal) - 1;
             sbal &= sbal - 1u;
             const int s0 = __shfl_sync(0xffffffffu, base, l), s1 = __shfl_sync(0xffffffffu, end, l);
-            for (int s = s0 + lane; s < s1; s += 32) {
-                const unsigned char meta = n.meta[s];
-                if (meta < 2) continue;
-                stdp_update<false>(n, s, (int)(meta >> 1) - 1, t, n.w[s]);
-            }
+            post_stdp_lane(n, s0 + lane, s1, t);
         }
         __syncwarp(); // the owners read these synapses at their next arrivals
     }
@@ -564,7 +666,7 @@ __global__ void __launch_bounds__(256, 3) k_update(NetDev n, int B) {
 // Propagate the spikes of the last B steps: one warp per spike, lanes over its
 // out-synapses; also appends the spikes to the run's raster in step order and
 // advances the device clock.  The last CTA to finish publishes the cursor.
-__global__ void __launch_bounds__(256, 2) k_propagate(NetDev n, int B) {
+__global__ void __launch_bounds__(256, 2) k_propagate(const __grid_constant__ NetDev n, int B) {
     __shared__ int pre[kMaxBlockSteps + 1];
     const int T0 = *n.tnow;
     const int run_t0 = *n.run_t0;
@@ -593,12 +695,15 @@ __global__ void __launch_bounds__(256, 2) k_propagate(NetDev n, int B) {
             else atomicOr(n.err, kErrOverflow);
         }
         const int q0 = n.out_ptr[src], q1 = n.out_ptr[src + 1];
+        // fire-and-forget reductions (no return value is used): the loads of
+        // later iterations do not wait on earlier atomics
+#pragma unroll 4
         for (int q = q0 + lane; q < q1; q += 32) {
             const unsigned int bit = n.out_bit[q];
             const unsigned int slot = (t + n.out_delay[q]) % (unsigned int)n.D;
             const unsigned int wd = bit >> 5;
-            const unsigned int old = atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
-            if (old == 0u) atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+            atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
+            atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
         }
     }
     if (blockIdx.x == 0 && (int)threadIdx.x < B) n.out_cnt[T0 - run_t0 + threadIdx.x] = n.blk_cnt[threadIdx.x];
