@@ -299,7 +299,7 @@ def bench_dense(args) -> dict:
     layer = NeuronLayer("TimeDrivenLIF_Voltage_jump", 1, parameters=dict(LIF_PARAMS))
     w64 = torch.from_numpy(w).double().cuda()
     out = {}
-    for prec in ("split_bf16", "fp32"):
+    for prec in ("split_bf16", "split_bf16_sync", "fp32"):
         eng = DensePopulations(w, layer, precision=prec)
         for _ in range(args.warmup):
             eng.run(per)
@@ -329,7 +329,7 @@ def bench_dense(args) -> dict:
     return _common(args, "steps/s", 1e3 / sp["ms_per_step"], "steps/s", sp["ms_per_step"] * per,
                    {"workload": "dense_split_bf16_64x8192", "instances": 64, "neurons": n, "sim_steps_per_step": per},
                    neuron_steps_per_s=64 * n * 1e3 / sp["ms_per_step"],
-                   roofline={"bound": "hbm", "kernel": "k_dense_gemm (split BF16, mma.sync)", "achieved": achieved,
+                   roofline={"bound": "hbm", "kernel": "k_dense_umma (split BF16, tcgen05)", "achieved": achieved,
                              "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind,
                              "traffic": None, "tflops": flops / (sp["delivery_us"] * 1e-6) / 1e12},
                    paths=out)

@@ -27,7 +27,10 @@
 extern "C" {
 #endif
 
-enum { NBG_DENSE_SPLIT_BF16 = 0, NBG_DENSE_FP32 = 1 };
+/* Delivery paths: SPLIT_BF16 = tcgen05 tensor cores (TMEM accumulator, bulk
+ * copies); FP32 = exact CUDA-core gather-sum; SPLIT_BF16_SYNC = the same
+ * split-precision GEMM on the legacy mma.sync tensor path (for comparison). */
+enum { NBG_DENSE_SPLIT_BF16 = 0, NBG_DENSE_FP32 = 1, NBG_DENSE_SPLIT_BF16_SYNC = 2 };
 
 typedef struct nbg_dense nbg_dense;
 

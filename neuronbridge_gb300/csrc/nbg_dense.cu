@@ -5,8 +5,12 @@
 //   delivery   I_t = S_{t-1} W          S binary, W N x N FP32
 //   update     voltage-jump LIF over B x N neurons, writes S_t
 //
-// Two delivery paths:
-//   * NBG_DENSE_SPLIT_BF16 -- tensor cores.  W = W_hi + W_lo with both parts
+// Delivery paths:
+//   * NBG_DENSE_SPLIT_BF16 -- tcgen05 (nbg_umma.cuh): the same split-K GEMM
+//     with the accumulator in tensor memory and operands in the UMMA blocked
+//     layout, moved by bulk copies; W is tiled once at create time and the
+//     update kernel writes S blocked.
+//   * NBG_DENSE_SPLIT_BF16_SYNC -- the legacy mma.sync tensor path.  W = W_hi + W_lo with both parts
 //     BF16 (W_hi = bf16(W), W_lo = bf16(W - W_hi)); a binary spike is exact in
 //     BF16, so S W_hi + S W_lo accumulated in FP32 carries ~16 mantissa bits
 //     of W.  The GEMM is "swap-AB": M = post-synaptic neurons (128 per CTA),
@@ -30,6 +34,7 @@
 
 #include "nbg_common.cuh"
 #include "nbg_dense.h"
+#include "nbg_umma.cuh"
 
 namespace {
 
@@ -62,6 +67,28 @@ __global__ void k_split_transpose(const float *__restrict__ w, __nv_bfloat16 *__
         hi[o] = h;
         lo[o] = l;
     }
+}
+
+// W (pre x post, FP32) -> W_hi^T, W_lo^T in the UMMA blocked layout: block
+// (m tile, k chunk) of 128 post x 64 pre at ((mt * kchunks + kc) * 16 KiB).
+__global__ void k_split_tile(const float *__restrict__ w, __nv_bfloat16 *__restrict__ hi,
+                             __nv_bfloat16 *__restrict__ lo, int n) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)n * n) return;
+    const int k = (int)(idx / n), j = (int)(idx % n); // W[k][j]: pre k, post j
+    const float x = w[idx];
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+    const int kchunks = n / umma::kKChunk;
+    const size_t byte = ((size_t)(j / umma::kM) * kchunks + k / umma::kKChunk) * umma::kBlockA +
+                        umma::block_offset(j % umma::kM, k % umma::kKChunk);
+    hi[byte / 2] = h;
+    lo[byte / 2] = l;
+}
+
+// offset (elements) of S[b][k] in the blocked S of the tcgen05 path
+__device__ __host__ __forceinline__ size_t s_blocked(int b, int k) {
+    return ((size_t)(k / umma::kKChunk) * umma::kBlockB + umma::block_offset(b, k % umma::kKChunk)) / 2;
 }
 
 // ------------------------------------------------------------- GEMM (mma.sync)
@@ -223,8 +250,9 @@ struct LifParams {
 // :49-86), spike -> S_t (BF16 0/1 for the tensor path, bit words for FP32).
 __global__ void __launch_bounds__(256) k_dense_lif(LifParams P, const float *__restrict__ partial, int nparts,
                                                    float *__restrict__ v, int *__restrict__ last,
-                                                   __nv_bfloat16 *__restrict__ s_out, unsigned *__restrict__ bits_out,
-                                                   int *__restrict__ counts, int t, int total) {
+                                                   __nv_bfloat16 *__restrict__ s_out, int s_blocked_layout,
+                                                   unsigned *__restrict__ bits_out, int *__restrict__ counts, int t,
+                                                   int n, int total) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     bool spk = false;
     if (idx < total) {
@@ -246,7 +274,11 @@ __global__ void __launch_bounds__(256) k_dense_lif(LifParams P, const float *__r
         }
         v[idx] = vv;
         last[idx] = ls;
-        if (s_out) s_out[idx] = __float2bfloat16_rn(spk ? 1.0f : 0.0f);
+        if (s_out) {
+            const __nv_bfloat16 one = __float2bfloat16_rn(spk ? 1.0f : 0.0f);
+            if (s_blocked_layout) s_out[s_blocked(idx / n, idx % n)] = one;
+            else s_out[idx] = one;
+        }
     }
     const unsigned bal = __ballot_sync(0xffffffffu, spk);
     if ((threadIdx.x & 31) == 0) {
@@ -263,7 +295,7 @@ struct nbg_dense {
     DevBuf<float> w, partial, v;
     DevBuf<__nv_bfloat16> whi, wlo, s[2];
     DevBuf<unsigned> bits[2];
-    DevBuf<int> last;
+    DevBuf<int> last, err;
     std::vector<cudaEvent_t> dev_pool; // delivery start/stop events, 2 per step
     int next_t = 0;
     bool ran = false;
@@ -295,6 +327,10 @@ nbg_status dense_reset(nbg_dense *d) {
 // delivery of S (buffer `par`) into d->partial (parts, instance-major)
 nbg_status launch_delivery(nbg_dense *d, int par) {
     if (d->precision == NBG_DENSE_SPLIT_BF16) {
+        dim3 grid(d->N / umma::kM, kSplitK);
+        umma::k_dense_umma<<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
+            d->whi.p, d->wlo.p, d->s[par].p, d->partial.p, d->N, kSplitK, d->err.p);
+    } else if (d->precision == NBG_DENSE_SPLIT_BF16_SYNC) {
         dim3 grid(d->N / kBM, kSplitK);
         k_dense_gemm<<<grid, kGemmThreads, kGemmSmem, d->stream>>>(d->whi.p, d->wlo.p, d->s[par].p, d->partial.p,
                                                                    d->N);
@@ -319,7 +355,7 @@ nbg_status nbg_dense_create(int instances, int neurons, const float *w, const nb
     if (neurons <= 0 || neurons % kBM != 0 || (neurons / kSplitK) % kBK != 0)
         return nbg_fail(NBG_ERR_INVALID, "neurons must be a positive multiple of %d", kBM);
     if (lif->model != NBG_MODEL_LIF_VJ) return nbg_fail(NBG_ERR_UNSUPPORTED, "the dense engine runs the voltage-jump LIF");
-    if (precision != NBG_DENSE_SPLIT_BF16 && precision != NBG_DENSE_FP32)
+    if (precision != NBG_DENSE_SPLIT_BF16 && precision != NBG_DENSE_FP32 && precision != NBG_DENSE_SPLIT_BF16_SYNC)
         return nbg_fail(NBG_ERR_INVALID, "unknown precision %d", precision);
     if (!(dt_ms > 0.0f) || !(lif->f[1] != 0.0f)) return nbg_fail(NBG_ERR_INVALID, "dt and tau must be non-zero");
     auto *d = new nbg_dense();
@@ -358,6 +394,8 @@ nbg_status nbg_dense_create(int instances, int neurons, const float *w, const nb
     chk(cudaEventCreate(&d->evd1));
     chk(d->v.alloc(tot));
     chk(d->last.alloc(tot));
+    chk(d->err.alloc(1));
+    chk(d->err.zero());
     chk(d->partial.alloc((size_t)kSplitK * tot));
     for (int k = 0; k < 2; ++k) {
         chk(d->s[k].alloc(tot));
@@ -372,7 +410,14 @@ nbg_status nbg_dense_create(int instances, int neurons, const float *w, const nb
         chk(d->whi.alloc(nn));
         chk(d->wlo.alloc(nn));
         if (ce == cudaSuccess) chk(cudaMemcpy(tmp.p, w, nn * sizeof(float), cudaMemcpyHostToDevice));
-        if (ce == cudaSuccess) {
+        if (ce == cudaSuccess && precision == NBG_DENSE_SPLIT_BF16) {
+            k_split_tile<<<(unsigned)((nn + 255) / 256), 256>>>(tmp.p, d->whi.p, d->wlo.p, neurons);
+            chk(cudaGetLastError());
+            chk(cudaDeviceSynchronize());
+            if (ce == cudaSuccess)
+                chk(cudaFuncSetAttribute(umma::k_dense_umma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         umma::kSmemBytes));
+        } else if (ce == cudaSuccess) {
             dim3 grid(neurons / 32, neurons / 32), block(32, 8);
             k_split_transpose<<<grid, block>>>(tmp.p, d->whi.p, d->wlo.p, neurons);
             chk(cudaGetLastError());
@@ -428,7 +473,8 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
     }
     double dms = 0.0;
     NBG_CUDA(cudaEventRecord(d->ev0, d->stream));
-    const bool tensor = d->precision == NBG_DENSE_SPLIT_BF16;
+    const bool tensor = d->precision != NBG_DENSE_FP32;
+    const int blocked = d->precision == NBG_DENSE_SPLIT_BF16;
     for (int k0 = 0; k0 < count; k0 += chunk) {
         const int k1 = std::min(count, k0 + chunk);
         for (int k = k0; k < k1; ++k) {
@@ -438,8 +484,8 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
             launch_delivery(d, in);
             NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0) + 1], d->stream));
             k_dense_lif<<<(total + 255) / 256, 256, 0, d->stream>>>(
-                d->P, d->partial.p, tensor ? kSplitK : 1, d->v.p, d->last.p, tensor ? d->s[outp].p : nullptr,
-                tensor ? nullptr : d->bits[outp].p, dcnt.p + k, t, total);
+                d->P, d->partial.p, tensor ? kSplitK : 1, d->v.p, d->last.p, tensor ? d->s[outp].p : nullptr, blocked,
+                tensor ? nullptr : d->bits[outp].p, dcnt.p + k, t, d->N, total);
         }
         NBG_CUDA(cudaGetLastError());
         NBG_CUDA(cudaEventSynchronize(d->dev_pool[2 * (k1 - 1 - k0) + 1]));
@@ -457,6 +503,9 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
     d->last_delivery_ms = dms;
     d->last_launches = 2LL * count;
     NBG_CUDA(cudaMemcpy(cnt.data(), dcnt.p, count * sizeof(int), cudaMemcpyDeviceToHost));
+    int errv = 0;
+    NBG_CUDA(cudaMemcpy(&errv, d->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (errv) return nbg_fail(NBG_ERR_TIMEOUT, "tensor-core delivery gave up waiting on a pipeline barrier");
     d->counts_host.insert(d->counts_host.end(), cnt.begin(), cnt.end());
     d->next_t += count;
     d->ran = true;
@@ -496,10 +545,14 @@ nbg_status nbg_dense_get_spikes(nbg_dense *d, uint8_t *s) {
         std::memset(s, 0, tot);
         return NBG_OK;
     }
-    if (d->precision == NBG_DENSE_SPLIT_BF16) {
+    if (d->precision != NBG_DENSE_FP32) {
         std::vector<__nv_bfloat16> h(tot);
         NBG_CUDA(cudaMemcpy(h.data(), d->s[par].p, tot * sizeof(__nv_bfloat16), cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < tot; ++i) s[i] = __bfloat162float(h[i]) != 0.0f;
+        const bool blocked = d->precision == NBG_DENSE_SPLIT_BF16;
+        for (size_t i = 0; i < tot; ++i) {
+            const size_t src = blocked ? s_blocked((int)(i / d->N), (int)(i % d->N)) : i;
+            s[i] = __bfloat162float(h[src]) != 0.0f;
+        }
     } else {
         std::vector<unsigned> h(tot / 32);
         NBG_CUDA(cudaMemcpy(h.data(), d->bits[par].p, (tot / 32) * sizeof(unsigned), cudaMemcpyDeviceToHost));
@@ -521,6 +574,14 @@ nbg_status nbg_dense_deliver(nbg_dense *d, const uint8_t *s, float *out) {
     NBG_CUDA(part.alloc((size_t)kSplitK * tot));
     if (d->precision == NBG_DENSE_SPLIT_BF16) {
         std::vector<__nv_bfloat16> h(tot);
+        for (size_t i = 0; i < tot; ++i)
+            h[s_blocked((int)(i / d->N), (int)(i % d->N))] = __float2bfloat16_rn(s[i] ? 1.0f : 0.0f);
+        NBG_CUDA(sb.upload(h));
+        dim3 grid(d->N / umma::kM, kSplitK);
+        umma::k_dense_umma<<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(d->whi.p, d->wlo.p, sb.p, part.p,
+                                                                               d->N, kSplitK, d->err.p);
+    } else if (d->precision == NBG_DENSE_SPLIT_BF16_SYNC) {
+        std::vector<__nv_bfloat16> h(tot);
         for (size_t i = 0; i < tot; ++i) h[i] = __float2bfloat16_rn(s[i] ? 1.0f : 0.0f);
         NBG_CUDA(sb.upload(h));
         dim3 grid(d->N / kBM, kSplitK);
@@ -535,14 +596,18 @@ nbg_status nbg_dense_deliver(nbg_dense *d, const uint8_t *s, float *out) {
     }
     NBG_CUDA(cudaGetLastError());
     NBG_CUDA(cudaStreamSynchronize(d->stream));
-    std::vector<float> h((size_t)(d->precision == NBG_DENSE_SPLIT_BF16 ? kSplitK : 1) * tot);
+    const bool split = d->precision != NBG_DENSE_FP32;
+    std::vector<float> h((size_t)(split ? kSplitK : 1) * tot);
     NBG_CUDA(cudaMemcpy(h.data(), part.p, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < tot; ++i) {
         float a = h[i];
-        if (d->precision == NBG_DENSE_SPLIT_BF16)
+        if (split)
             for (int k = 1; k < kSplitK; ++k) a = a + h[(size_t)k * tot + i];
         out[i] = a;
     }
+    int errv = 0;
+    NBG_CUDA(cudaMemcpy(&errv, d->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (errv) return nbg_fail(NBG_ERR_TIMEOUT, "tensor-core delivery gave up waiting on a pipeline barrier");
     return NBG_OK;
 }
 

@@ -3,8 +3,9 @@
 Wraps the C ABI in ``include/nbg_dense.h``: 64 instances of an N-neuron
 voltage-jump LIF population share one dense weight matrix W (row = pre,
 column = post); each step delivers I = S W either as a BF16 split-precision
-tensor-core GEMM (``precision="split_bf16"``) or as an exact FP32 CUDA-core
-gather-sum (``precision="fp32"``).
+tensor-core GEMM on tcgen05 (``precision="split_bf16"``), the same GEMM on
+the legacy mma.sync path (``"split_bf16_sync"``), or as an exact FP32
+CUDA-core gather-sum (``"fp32"``).
 """
 from __future__ import annotations
 
@@ -15,7 +16,7 @@ import numpy as np
 from . import _lib
 from .model import NeuronLayer
 
-PRECISIONS = {"split_bf16": 0, "fp32": 1}
+PRECISIONS = {"split_bf16": 0, "fp32": 1, "split_bf16_sync": 2}
 
 _SIG = {
     "nbg_dense_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float),

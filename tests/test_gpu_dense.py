@@ -1,5 +1,6 @@
-"""Dense all-to-all delivery (split-precision tensor-core GEMM and the FP32
-CUDA-core path) against the CPU oracle and an FP64 product.
+"""Dense all-to-all delivery (split-precision tensor-core GEMM on tcgen05 and
+on the legacy mma.sync path, and the FP32 CUDA-core path) against the CPU
+oracle and an FP64 product.
 
 Tolerances: the FP32 path is bit-exact (same ascending-i sequential sum as the
 oracle).  The split BF16 path (W = W_hi + W_lo, binary S exact in BF16, FP32
@@ -32,12 +33,13 @@ def _sequential_f32(w, s):
     return out
 
 
+@pytest.mark.parametrize("precision", ["split_bf16", "split_bf16_sync"])
 @pytest.mark.parametrize("n", [1024, 2048])
-def test_split_bf16_delivery_error_vs_fp64(n):
+def test_split_bf16_delivery_error_vs_fp64(n, precision):
     w = dense_weights(n, seed=4)
     rng = np.random.default_rng(7)
     s = (rng.random((64, n)) < 0.03).astype(np.uint8)
-    eng = DensePopulations(w, _layer(), precision="split_bf16")
+    eng = DensePopulations(w, _layer(), precision=precision)
     got = eng.deliver(s)
     ref = s.astype(np.float64) @ w.astype(np.float64)
     err = np.abs(got.astype(np.float64) - ref)
@@ -74,10 +76,20 @@ def test_fp32_simulation_bit_exact_vs_oracle(oracle_lib):
     assert np.array_equal(eng.spikes().ravel(), rs)
 
 
-def test_split_bf16_simulation_tracks_fp32():
+def test_tcgen05_and_mma_sync_paths_agree():
+    n = 2048
+    w = dense_weights(n, seed=4)
+    s = (np.random.default_rng(9).random((64, n)) < 0.05).astype(np.uint8)
+    a = DensePopulations(w, _layer(), precision="split_bf16").deliver(s)
+    b = DensePopulations(w, _layer(), precision="split_bf16_sync").deliver(s)
+    assert np.abs(a - b).max() < SPLIT_ABS_TOL
+
+
+@pytest.mark.parametrize("precision", ["split_bf16", "split_bf16_sync"])
+def test_split_bf16_simulation_tracks_fp32(precision):
     n, steps = 2048, 400
     w = dense_weights(n, seed=4)
-    a = DensePopulations(w, _layer(), precision="split_bf16").run(steps)
+    a = DensePopulations(w, _layer(), precision=precision).run(steps)
     b = DensePopulations(w, _layer(), precision="fp32").run(steps)
     ca, cb = a.spike_counts(), b.spike_counts()
     assert len(ca) == len(cb) == steps + 1

@@ -3,9 +3,10 @@ call cudaMalloc (a host that owns all device memory, a real-time control
 loop, code inside a global-mode stream capture).
 
 It is checked through the C ABI against the allocating entry point
-(nbg_dense_deliver) on the same weights and spikes, on two calls in a row,
-within the split-BF16 tolerance the dense tests use (2e-5 absolute; the two
-paths run the same kernel and summation order, so they agree exactly).  This
+(nbg_dense_deliver of an engine on the mma.sync split-BF16 path) on the same
+weights and spikes, on two calls in a row, within the split-BF16 tolerance the
+dense tests use (2e-5 absolute; both run the same kernel and summation order,
+so they agree exactly).  This
 file is collected last, and the test also passes alone in a fresh process.
 """
 import ctypes
@@ -38,7 +39,7 @@ def test_noalloc_delivery_matches_allocating_entry_point():
     n = 1024
     w = dense_weights(n, seed=4)
     eng = DensePopulations(w, NeuronLayer("TimeDrivenLIF_Voltage_jump", 1, parameters=dict(LIF_PARAMS)),
-                           precision="split_bf16")
+                           precision="split_bf16_sync")
     wt = torch.from_numpy(w).cuda()
     w_hi = wt.to(torch.bfloat16)
     w_lo = (wt - w_hi.float()).to(torch.bfloat16)
