@@ -54,6 +54,9 @@ BYTES_PER_NEURON_STEP = 32
 BYTES_PER_PLASTIC_EVENT = 40
 BYTES_PER_STATIC_EVENT = 12
 BYTES_PER_POST_UPDATE = 36
+# DRAM bytes (read + write) of one k_update launch of this workload (10 steps x
+# 100k neurons) from an ncu capture of that launch with a cold L2
+KUPDATE_TRAFFIC_BYTES = 56.5e6
 
 
 def _peaks():
@@ -496,7 +499,10 @@ def main() -> None:
         "roofline": {"bound": "hbm", "kernel": "k_update (drain + RK4 + STDP)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
-                     "traffic": None, "update_ms_share": tot_upd / tot_dev if tot_dev else None,
+                     "traffic": KUPDATE_TRAFFIC_BYTES if args.sim_steps % 10 == 0 else None,
+                     "traffic_unit": "bytes per launch (ncu, cold L2)",
+                     "algorithmic_bytes_per_launch": upd_bytes / max(1, launches // 2),
+                     "update_ms_share": tot_upd / tot_dev if tot_dev else None,
                      "propagate_ms_share": tot_prop / tot_dev if tot_dev else None,
                      "avg_update_launch_us": 1e6 * tot_upd / max(1, launches // 2)},
         "e2e": {"value": tot_ev_all / tot_wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 4 + 8 + 4,

@@ -119,8 +119,7 @@ struct NetDev {
     long long *cursor;
     long long out_cap;
     int *err;
-    int *tnow, *run_t0;
-    unsigned int *done;
+    int *run_t0;
     const int *trace_slot;
     float *trace;
     int ntrace;
@@ -277,56 +276,71 @@ constexpr int kPostChunk = 2;
 // [s, s1) of a spiking neuron, striding by the warp size.
 __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t);
 
-// Apply c <= kArrivalChunk arrivals s[0..c) of one target, in order: the
-// target's ProcessSpike with the weight as it is before this step's pre
-// hook, then the pre hooks of the plastic ones.  Synapse loads are batched.
-__device__ __forceinline__ void apply_arrivals(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
-                                               float &acc_b, bool gate, const int (&s)[kArrivalChunk], int c,
-                                               int t) {
-    unsigned char meta[kArrivalChunk];
-    float w[kArrivalChunk];
-#pragma unroll
-    for (int k = 0; k < kArrivalChunk; ++k) {
-        meta[k] = 0;
-        w[k] = 0.0f;
-        if (k < c) {
-            meta[k] = n.meta[s[k]];
-            w[k] = n.w[s[k]];
+// Apply one arrival on synapse s of a target: its ProcessSpike with the
+// weight as it is before this step's pre hook, then the pre hook if the
+// synapse is plastic.  The STDP state is loaded speculatively together with
+// meta and weight (one memory round trip), then the decay-table entry.
+__device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                              float &acc_b, bool gate, int s, int t) {
+    const unsigned char meta = n.meta[s];
+    const float w = n.w[s];
+    int last = 0;
+    float apre = 0.0f, apost = 0.0f, wmax = 0.0f;
+    if (n.apre) { // the network has plastic synapses: state arrays exist for every synapse
+        last = n.slast[s];
+        apre = n.apre[s];
+        apost = n.apost[s];
+        wmax = n.wmax[s];
+    }
+    const int type = meta & 1;
+    switch (M.model) {
+    case NBG_MODEL_LIF_VJ:
+        if (n.semantics == NBG_SEM_DENSE) {
+            if (type == 0) acc_a = acc_a + w;
+            else acc_b = acc_b + w;
+        } else if (gate) {
+            r.v = r.v + (type ? -w : w);
+        }
+        break;
+    case NBG_MODEL_IZH_COND:
+        if (n.semantics == NBG_SEM_DENSE) { // summed into the step's pending channels
+            if (type == 0) acc_a = acc_a + w;
+            else acc_b = acc_b + w;
+        } else if (type == 0) {
+            r.gexc = r.gexc + w;
+        } else {
+            r.ginh = r.ginh + w;
+        }
+        break;
+    default: // IZH_RK4 current pulse, POISSON rate increment
+        acc_a = acc_a + (type ? -w : w);
+        break;
+    }
+    if (n.ev_t) {
+        const unsigned long long pos = atomicAdd(n.ev_cursor, 1ull);
+        if (pos < (unsigned long long)n.ev_cap) {
+            n.ev_t[pos] = t;
+            n.ev_pos[pos] = s;
+            n.ev_w[pos] = w;
+        } else {
+            atomicOr(n.err, kErrEventLog);
         }
     }
-#pragma unroll
-    for (int k = 0; k < kArrivalChunk; ++k) {
-        if (k >= c) break;
-        const int type = meta[k] & 1;
-        switch (M.model) {
-        case NBG_MODEL_LIF_VJ:
-            if (n.semantics == NBG_SEM_DENSE) {
-                if (type == 0) acc_a = acc_a + w[k];
-                else acc_b = acc_b + w[k];
-            } else if (gate) {
-                r.v = r.v + (type ? -w[k] : w[k]);
-            }
-            break;
-        case NBG_MODEL_IZH_COND:
-            if (type == 0) r.gexc = r.gexc + w[k];
-            else r.ginh = r.ginh + w[k];
-            break;
-        default: // IZH_RK4 current pulse, POISSON rate increment
-            acc_a = acc_a + (type ? -w[k] : w[k]);
-            break;
+    if (meta >= 2) { // pre-synaptic pair STDP (STDP::ApplyPreSynaticSpike)
+        const int rule = (int)(meta >> 1) - 1;
+        const int gap = t - last;
+        float fp = 0.0f, fm = 0.0f;
+        if (gap < n.dtab_len) {
+            fp = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + gap]);
+            fm = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + gap]);
         }
-        if (n.ev_t) {
-            const unsigned long long pos = atomicAdd(n.ev_cursor, 1ull);
-            if (pos < (unsigned long long)n.ev_cap) {
-                n.ev_t[pos] = t;
-                n.ev_pos[pos] = s[k];
-                n.ev_w[pos] = w[k];
-            } else {
-                atomicOr(n.err, kErrEventLog);
-            }
-        }
+        const float a = __ldg(&n.rule_a[rule * 2 + 1]);
+        const float xpre = apre * fp + 1.0f, xpost = apost * fm;
+        n.apre[s] = xpre;
+        n.apost[s] = xpost;
+        n.slast[s] = t;
+        n.w[s] = clamp_w(w + (-a * xpost), wmax);
     }
-    stdp_batch<true, kArrivalChunk>(n, s, meta, w, t);
 }
 
 // Apply every set bit of `word` (word index wi of this target) in ascending
@@ -335,17 +349,15 @@ __device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, Neur
                                            float &acc_b, bool gate, unsigned int word, int first, int t) {
     while (word) {
         int sp[kArrivalChunk];
-        int c = 0;
 #pragma unroll
         for (int k = 0; k < kArrivalChunk; ++k) {
             sp[k] = first;
             if (word) {
                 sp[k] = first + __ffs(word) - 1;
                 word &= word - 1u;
-                c = k + 1;
+                apply_arrival(n, M, r, acc_a, acc_b, gate, sp[k], t);
             }
         }
-        apply_arrivals(n, M, r, acc_a, acc_b, gate, sp, c, t);
     }
 }
 
@@ -395,6 +407,29 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
         return false;
     }
     case NBG_MODEL_IZH_COND: {
+        if (n.semantics == NBG_SEM_DENSE) {
+            // dense runtime (DenseIzhikevichExponentialDecayDeviceUpdate.cuh:10-68):
+            // decay-then-add conductances, u from the new v, no refractory gate
+            const float ge = r.gexc * M.p[8] + acc_a;
+            const float gi = r.ginh * M.p[9] + acc_b;
+            const float V = r.v, U = r.u;
+            const float total = ge * (M.p[6] - V) + gi * (M.p[7] - V) + r.iext;
+            float v = V + n.dt * (0.04f * V * V + 5.0f * V + 140.0f - U + M.p[5] * total);
+            float u = U + n.dt * (M.p[0] * (M.p[1] * v - U));
+            r.gexc = ge;
+            r.ginh = gi;
+            r.last += 1;
+            bool s = false;
+            if (v >= M.p[4]) {
+                v = M.p[2];
+                u = u + M.p[3];
+                r.last = 0;
+                s = true;
+            }
+            r.v = v;
+            r.u = u;
+            return s;
+        }
         const float V = r.v, U = r.u;
         float total = 0.0f;
         if (M.flags & 1) total = total + r.gexc * (M.p[6] - V);
@@ -459,15 +494,31 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
     }
 }
 
-__device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts) {
-    if (ts < 0) return false;
+// Firing probability and local hash index of generator neuron k; constant
+// within a launch (its rate has no inputs; I_ext changes only between runs).
+__device__ __forceinline__ float generator_prob(const NetDev &n, int k, int *local) {
     const LayerDev &G = n.layers[n.pop[k]];
     float rate = G.f[0] + 0.0f + G.f[1] * n.iext[k];
     rate = rate > 0.0f ? rate : 0.0f;
     float prob = rate * n.dt * 0.001f;
-    prob = prob < 1.0f ? prob : 1.0f;
-    return hash_uniform01(k - G.start, ts) < prob;
+    *local = k - G.start;
+    return prob < 1.0f ? prob : 1.0f;
 }
+
+__device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts) {
+    if (ts < 0) return false;
+    int local;
+    const float prob = generator_prob(n, k, &local);
+    return hash_uniform01(local, ts) < prob;
+}
+
+// The first kGenCached generator inputs of a target, hoisted out of the step
+// loop: local hash index, delay, CSC rank and probability.
+constexpr int kGenCached = 1;
+struct GenIn {
+    int local, delay, pos;
+    float prob;
+};
 
 // Advance every neuron B steps (drain arrivals, integrate, compact spikes,
 // post-synaptic STDP).  One thread per neuron; all lanes stay in the loop so
@@ -507,12 +558,23 @@ __device__ __forceinline__ void summary_clear_range(unsigned int *srow, int woff
     }
 }
 
-__global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B) {
+// Launch parameters of one block of steps: B steps starting toff steps
+// after the run's first step; par = the block's parity (its spike counters);
+// bprev = the previous block's step count (0 for the first block of a run).
+__global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B, int toff, int par,
+                                                  int bprev) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = j < n.N;
     const int lane = threadIdx.x & 31;
-    const int T0 = *n.tnow;
     const int run_t0 = *n.run_t0;
+    const int T0 = run_t0 + toff;
+    int *cnt = n.blk_cnt + par * kMaxBlockSteps;
+    if (j == 0 && bprev > 0) { // publish the previous block's raster length
+        const int *prev = n.blk_cnt + (par ^ 1) * kMaxBlockSteps;
+        long long add = 0;
+        for (int b = 0; b < bprev; ++b) add += prev[b];
+        *n.cursor += add;
+    }
 
     Model L;
     NeuronRegs r;
@@ -535,6 +597,19 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
         g1 = n.gen_ptr[j + 1];
         // compacted if its spikes are recorded or must be propagated
         listed = L.record || n.out_ptr[j + 1] > n.out_ptr[j];
+    }
+    GenIn gin[kGenCached];
+#pragma unroll
+    for (int q = 0; q < kGenCached; ++q) {
+        gin[q].local = 0;
+        gin[q].delay = 0;
+        gin[q].pos = 0;
+        gin[q].prob = -1.0f; // never fires
+        if (active && g0 + q < g1) {
+            gin[q].prob = generator_prob(n, n.gen_src[g0 + q], &gin[q].local);
+            gin[q].delay = n.gen_delay[g0 + q];
+            gin[q].pos = n.gen_pos[g0 + q];
+        }
     }
     float nz[kMaxBlockSteps];
     if (active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f) {
@@ -585,7 +660,15 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
                 }
                 // generator arrivals of this step (pure functions of source and time)
                 unsigned int gfired = 0u, gwords = 0u;
-                for (int g = g0; g < g1; ++g)
+#pragma unroll
+                for (int q = 0; q < kGenCached; ++q) {
+                    const int ts = t - gin[q].delay;
+                    if (ts >= 0 && hash_uniform01(gin[q].local, ts) < gin[q].prob) {
+                        gfired |= 1u << q;
+                        gwords |= 1u << (gin[q].pos >> 5);
+                    }
+                }
+                for (int g = g0 + kGenCached; g < g1; ++g)
                     if (generator_fired(n, n.gen_src[g], t - (int)n.gen_delay[g])) {
                         gfired |= 1u << (g - g0);
                         gwords |= 1u << (n.gen_pos[g] >> 5);
@@ -608,7 +691,8 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
                         mrow[wi] = 0u;
                     }
                     for (unsigned int gf = gfired; gf; gf &= gf - 1u) {
-                        const int gp = n.gen_pos[g0 + __ffs(gf) - 1];
+                        const int q = __ffs(gf) - 1;
+                        const int gp = q == 0 ? gin[0].pos : n.gen_pos[g0 + q];
                         if ((gp >> 5) == wi) word |= 1u << (gp & 31);
                     }
                     delivered += __popc(word);
@@ -636,7 +720,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
         if (bal) {
             const int leader = __ffs(bal) - 1;
             int pos = 0;
-            if (lane == leader) pos = atomicAdd(&n.blk_cnt[b], __popc(bal));
+            if (lane == leader) pos = atomicAdd(&cnt[b], __popc(bal));
             pos = __shfl_sync(0xffffffffu, pos, leader);
             if (spk && listed) n.blk_spk[(size_t)b * n.N + pos + __popc(bal & ((1u << lane) - 1u))] = j;
         }
@@ -664,17 +748,18 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
 }
 
 // Propagate the spikes of the last B steps: one warp per spike, lanes over its
-// out-synapses; also appends the spikes to the run's raster in step order and
-// advances the device clock.  The last CTA to finish publishes the cursor.
-__global__ void __launch_bounds__(256, 2) k_propagate(const __grid_constant__ NetDev n, int B) {
+// out-synapses; also appends the spikes to the run's raster in step order at
+// the cursor the next update launch advances.  CTA 0 records the per-step
+// counts and clears the other parity's counters for the next block.
+__global__ void __launch_bounds__(256, 2) k_propagate(const __grid_constant__ NetDev n, int B, int toff, int par) {
     __shared__ int pre[kMaxBlockSteps + 1];
-    const int T0 = *n.tnow;
-    const int run_t0 = *n.run_t0;
+    const int T0 = *n.run_t0 + toff;
+    const int *cnt = n.blk_cnt + par * kMaxBlockSteps;
     if (threadIdx.x == 0) {
         int s = 0;
         for (int b = 0; b < B; ++b) {
             pre[b] = s;
-            s += n.blk_cnt[b];
+            s += cnt[b];
         }
         pre[B] = s;
     }
@@ -706,19 +791,9 @@ __global__ void __launch_bounds__(256, 2) k_propagate(const __grid_constant__ Ne
             atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
         }
     }
-    if (blockIdx.x == 0 && (int)threadIdx.x < B) n.out_cnt[T0 - run_t0 + threadIdx.x] = n.blk_cnt[threadIdx.x];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned int prev = atomicAdd(n.done, 1u);
-        if (prev == gridDim.x - 1) {
-            __threadfence();
-            *n.cursor = cur + total;
-            for (int b = 0; b < B; ++b) n.blk_cnt[b] = 0;
-            *n.tnow = T0 + B;
-            *n.done = 0u;
-            __threadfence();
-        }
+    if (blockIdx.x == 0 && (int)threadIdx.x < kMaxBlockSteps) {
+        if ((int)threadIdx.x < B) n.out_cnt[toff + threadIdx.x] = cnt[threadIdx.x];
+        n.blk_cnt[(par ^ 1) * kMaxBlockSteps + threadIdx.x] = 0;
     }
 }
 
@@ -756,9 +831,9 @@ struct nbg_engine {
     DevBuf<float> v, u, gexc, ginh, iext, w, wmax, apre, apost, dtab, rule_a, trace, ev_w;
     DevBuf<int> gen_ptr, gen_pos, gen_src;
     DevBuf<unsigned short> gen_delay;
-    DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, blk_spk, blk_cnt, out_ids, out_cnt, err, tnow, run_t0,
+    DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, blk_spk, blk_cnt, out_ids, out_cnt, err, run_t0,
         trace_slot, ev_t, ev_pos;
-    DevBuf<unsigned int> mask, wsum, out_bit, done;
+    DevBuf<unsigned int> mask, wsum, out_bit;
     int Ws = 1;
     DevBuf<unsigned short> out_delay;
     DevBuf<long long> cursor;
@@ -838,9 +913,7 @@ struct nbg_engine {
         n.cursor = cursor.p;
         n.out_cap = (long long)out_ids.n;
         n.err = err.p;
-        n.tnow = tnow.p;
         n.run_t0 = run_t0.p;
-        n.done = done.p;
         n.trace_slot = trace_ids.empty() ? nullptr : trace_slot.p;
         n.trace = trace.p;
         n.ntrace = (int)trace_ids.size();
@@ -916,8 +989,6 @@ nbg_status reset_state(nbg_engine *e) {
     NBG_CUDA(e->wsum.zero());
     NBG_CUDA(e->blk_cnt.zero());
     NBG_CUDA(e->err.zero());
-    NBG_CUDA(e->tnow.zero());
-    NBG_CUDA(e->done.zero());
     NBG_CUDA(e->cursor.zero());
     NBG_CUDA(e->ev_cursor.zero());
     NBG_CUDA(e->n_events.zero());
@@ -951,13 +1022,14 @@ nbg_status ensure_timing_events(nbg_engine *e, int blocks) {
 // triple bracketing the two kernels.
 // Inside stream capture an event record must be "external" to become an
 // event-record node of the graph (a plain record is only a dependency).
-void launch_block(nbg_engine *e, const NetDev &nd, int B, int slot, bool capturing = false) {
+void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int par, int bprev, int slot,
+                  bool capturing = false) {
     const int grid = (e->N + e->threads - 1) / e->threads;
     const unsigned int flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 0], e->stream, flags);
-    k_update<<<grid, e->threads, 0, e->stream>>>(nd, B);
+    k_update<<<grid, e->threads, 0, e->stream>>>(nd, B, toff, par, bprev);
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 1], e->stream, flags);
-    k_propagate<<<e->prop_grid, 256, 0, e->stream>>>(nd, B);
+    k_propagate<<<e->prop_grid, 256, 0, e->stream>>>(nd, B, toff, par);
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 2], e->stream, flags);
 }
 
@@ -1061,10 +1133,16 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
         std::memcpy(L.f, ld.f, sizeof(L.f));
         std::memcpy(L.ip, ld.ip, sizeof(L.ip));
         if (ld.model == NBG_MODEL_IZH_COND) {
-            const float inv_a = ld.f[8] != 0.0f ? 1.0f / ld.f[8] : 0.0f;
-            const float inv_g = ld.f[10] != 0.0f ? 1.0f / ld.f[10] : 0.0f;
-            L.decay_exc = std::exp(-d->dt_ms * inv_a);
-            L.decay_inh = std::exp(-d->dt_ms * inv_g);
+            if (d->semantics == NBG_SEM_DENSE) {
+                // dense runtime: std::exp(-dt_ms / tau) (DenseIzhikevichExponentialDecayModel.h:139-141)
+                L.decay_exc = std::exp(-d->dt_ms / ld.f[8]);
+                L.decay_inh = std::exp(-d->dt_ms / ld.f[10]);
+            } else {
+                const float inv_a = ld.f[8] != 0.0f ? 1.0f / ld.f[8] : 0.0f;
+                const float inv_g = ld.f[10] != 0.0f ? 1.0f / ld.f[10] : 0.0f;
+                L.decay_exc = std::exp(-d->dt_ms * inv_a);
+                L.decay_inh = std::exp(-d->dt_ms * inv_g);
+            }
         }
         if (ld.model == NBG_MODEL_LIF_VJ) {
             if (!(ld.f[1] != 0.0f)) return bail(fail(NBG_ERR_INVALID, "layer %d: tau must be non-zero", l));
@@ -1252,11 +1330,9 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(e->gen_src.upload(gsrc), "gen_src");
     chk(e->gen_delay.upload(gdelay), "gen_delay");
     chk(e->blk_spk.alloc((size_t)kMaxBlockSteps * N), "block spike lists");
-    chk(e->blk_cnt.alloc(kMaxBlockSteps), "block counts");
+    chk(e->blk_cnt.alloc(2 * kMaxBlockSteps), "block counts");
     chk(e->err.alloc(1), "err");
-    chk(e->tnow.alloc(1), "tnow");
     chk(e->run_t0.alloc(1), "run_t0");
-    chk(e->done.alloc(1), "done");
     chk(e->cursor.alloc(1), "cursor");
     chk(e->ev_cursor.alloc(1), "ev_cursor");
     chk(e->n_events.alloc(1), "n_events");
@@ -1280,7 +1356,9 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     if (st != NBG_OK) return bail(st);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
-    e->prop_grid = std::max(1, sms) * 2;
+    // propagate CTAs: one per SM for small networks, up to 8 per SM for large
+    // ones (more spikes per block than warps otherwise)
+    e->prop_grid = std::max(std::max(1, sms), std::min(std::max(1, sms) * 8, e->N / 4096));
     e->spike_capacity = opt.spike_capacity;
     *out = e;
     return NBG_OK;
@@ -1326,6 +1404,7 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     const int t0 = e->next_t;
     NBG_CUDA(cudaMemcpyAsync(e->run_t0.p, &t0, sizeof(int), cudaMemcpyHostToDevice, e->stream));
     NBG_CUDA(cudaMemsetAsync(e->cursor.p, 0, sizeof(long long), e->stream));
+    NBG_CUDA(cudaMemsetAsync(e->blk_cnt.p, 0, 2 * kMaxBlockSteps * sizeof(int), e->stream));
     NBG_CUDA(cudaMemsetAsync(e->err.p, 0, sizeof(int), e->stream));
     const NetDev nd = e->dev();
 
@@ -1359,8 +1438,8 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
             }
             cudaGraph_t g;
             NBG_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < nfull; ++k) launch_block(e, nd, B, k, true);
-            if (tail) launch_block(e, nd, tail, nfull, true);
+            for (int k = 0; k < nfull; ++k) launch_block(e, nd, B, k * B, k & 1, k ? B : 0, k, true);
+            if (tail) launch_block(e, nd, tail, nfull * B, nfull & 1, nfull ? B : 0, nfull, true);
             NBG_CUDA(cudaStreamEndCapture(e->stream, &g));
             cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
             cudaGraphDestroy(g);
@@ -1381,6 +1460,7 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         if (ps != NBG_OK) return ps;
         int t = t0;
         size_t ci = 0;
+        int nlaunch = 0, bprev = 0;
         while (t < t_end) {
             while (ci < due.size() && due[ci].t == t) {
                 NBG_CUDA(cudaMemcpyAsync(e->iext.p + due[ci].id, &due[ci].value, sizeof(float),
@@ -1393,7 +1473,10 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
             const int nblocks = (seg + B - 1) / B;
             int slot = 0;
             for (int k = 0; k < nblocks; ++k) {
-                launch_block(e, nd, std::min(B, seg - k * B), slot++);
+                const int bk = std::min(B, seg - k * B);
+                launch_block(e, nd, bk, t + k * B - t0, nlaunch & 1, bprev, slot++);
+                bprev = bk;
+                ++nlaunch;
                 launches += 2;
                 if (slot == kLaunchChunk) {
                     nbg_status hs = harvest_timing(e, slot);
@@ -1415,9 +1498,7 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     e->last_launches = launches;
 
     int errv = 0;
-    long long nspk = 0;
     NBG_CUDA(cudaMemcpy(&errv, e->err.p, sizeof(int), cudaMemcpyDeviceToHost));
-    NBG_CUDA(cudaMemcpy(&nspk, e->cursor.p, sizeof(long long), cudaMemcpyDeviceToHost));
     e->next_t += count;
     e->ran = true;
     if (errv & kErrEventLog) return fail(NBG_ERR_OVERFLOW, "delivered-event log capacity exceeded");
@@ -1426,6 +1507,8 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     // raster: per-step counts and ids, sorted by id within a step
     std::vector<int> cnt((size_t)count);
     NBG_CUDA(cudaMemcpy(cnt.data(), e->out_cnt.p, count * sizeof(int), cudaMemcpyDeviceToHost));
+    long long nspk = 0;
+    for (int c : cnt) nspk += c;
     const size_t base = e->spk_id.size();
     e->spk_id.resize(base + (size_t)nspk);
     e->spk_t.resize(base + (size_t)nspk);

@@ -83,6 +83,7 @@ typedef struct {
     int *layer_of; /* neuron -> layer index */
     /* neuron state (SoA) */
     REAL *v, *u, *g_ampa, *g_gaba, *i_ext, *rate;
+    REAL *pend_e, *pend_i; /* dense profile: arrivals of the current step */
     int *last;
     /* synapses in CSC order (by target, source, delay, original index) */
     int64_t n_syn;
@@ -305,6 +306,8 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
     n->g_gaba = (REAL *)calloc(nn, sizeof(REAL));
     n->i_ext = (REAL *)calloc(nn, sizeof(REAL));
     n->rate = (REAL *)calloc(nn, sizeof(REAL));
+    n->pend_e = (REAL *)calloc(nn, sizeof(REAL));
+    n->pend_i = (REAL *)calloc(nn, sizeof(REAL));
     n->last = (int *)malloc(nn * sizeof(int));
     n->fired = (unsigned char *)calloc(nn, 1);
     n->threads = 1;
@@ -340,7 +343,11 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
              * (TimeDrivenIzhikevic_Exponential_Decay.cpp:32-39) */
             float inv_a = (float)L->f[8] != 0.0f ? 1.0f / (float)L->f[8] : 0.0f;
             float inv_g = (float)L->f[10] != 0.0f ? 1.0f / (float)L->f[10] : 0.0f;
-            if (sizeof(REAL) == sizeof(float)) {
+            if (sizeof(REAL) == sizeof(float) && semantics == SEM_DENSE) {
+                /* dense runtime: std::exp(-dt_ms / tau) (DenseIzhikevichExponentialDecayModel.h:139-141) */
+                L->decay_ampa = (REAL)expf(-dt / (float)L->f[8]);
+                L->decay_gaba = (REAL)expf(-dt / (float)L->f[10]);
+            } else if (sizeof(REAL) == sizeof(float)) {
                 L->decay_ampa = (REAL)expf(-dt * inv_a);
                 L->decay_gaba = (REAL)expf(-dt * inv_g);
             } else {
@@ -363,6 +370,8 @@ void ORC(destroy)(void *hp) {
     free(n->g_gaba);
     free(n->i_ext);
     free(n->rate);
+    free(n->pend_e);
+    free(n->pend_i);
     free(n->last);
     free(n->csc_ptr);
     free(n->csc_src);
@@ -470,8 +479,12 @@ static void deliver(net_t *n, int64_t p, int t) {
         }
         break;
     case M_IZH_COND:
-        /* g += w, not gated (TimeDrivenIzhikevic_Exponential_Decay.cpp:119-131) */
-        if (type == 0) n->g_ampa[j] += w;
+        /* legacy: g += w, not gated (TimeDrivenIzhikevic_Exponential_Decay.cpp:119-131);
+         * dense profile: summed into the step's pending channels (i_pend) */
+        if (n->semantics == SEM_DENSE) {
+            if (type == 0) n->pend_e[j] += w;
+            else n->pend_i[j] += w;
+        } else if (type == 0) n->g_ampa[j] += w;
         else n->g_gaba[j] += w;
         break;
     case M_IZH_RK4:
@@ -526,7 +539,35 @@ static int spiked_lif(net_t *n, layer_t *L, int i) {
     return 0;
 }
 
+/* Dense-runtime Izhikevich (gpu DenseIzhikevichExponentialDecayDeviceUpdate.cuh
+ * :10-68, DenseIntegrationKernels.cuh:10-75): decay-then-add conductances,
+ * Euler step with u updated from the new v, no refractory gate. */
+static int spiked_izh_dense(net_t *n, layer_t *L, int i) {
+    const REAL ge = n->g_ampa[i] * L->decay_ampa + n->pend_e[i];
+    const REAL gi = n->g_gaba[i] * L->decay_gaba + n->pend_i[i];
+    n->pend_e[i] = 0;
+    n->pend_i[i] = 0;
+    const REAL V = n->v[i], U = n->u[i];
+    const REAL total = ge * (L->f[7] - V) + gi * (L->f[9] - V) + n->i_ext[i];
+    REAL v = V + n->dt * (K(0.04) * V * V + K(5.0) * V + K(140.0) - U + L->f[6] * total);
+    REAL u = U + n->dt * (L->f[0] * (L->f[1] * v - U));
+    n->g_ampa[i] = ge;
+    n->g_gaba[i] = gi;
+    n->last[i] += 1;
+    int s = 0;
+    if (v >= L->f[5]) {
+        v = L->f[2];
+        u += L->f[3];
+        n->last[i] = 0;
+        s = 1;
+    }
+    n->v[i] = v;
+    n->u[i] = u;
+    return s;
+}
+
 static int spiked_izh_cond(net_t *n, layer_t *L, int i) {
+    if (n->semantics == SEM_DENSE) return spiked_izh_dense(n, L, i);
     /* TimeDrivenIzhikevic_Exponential_Decay.cpp:59-110 */
     const REAL V = n->v[i], U = n->u[i];
     REAL total = K(0.0);

@@ -139,6 +139,31 @@ def test_dense_semantics_profile(oracle_lib):
     assert np.array_equal(sim.state_field(0), o.state(0).astype(np.float32))
 
 
+def test_dense_semantics_izhikevich(oracle_lib):
+    """Dense-runtime Izhikevich (decay-then-add, u from the new v, V_th given)
+    driven by Poisson sources through excitatory and inhibitory synapses."""
+    rng = np.random.default_rng(12)
+    n, npoi = 400, 200
+    net = nb.Network()
+    net.add_layer(nb.NeuronLayer("TimeDrivenIzhikevic_Exponential_Decay", n, output=True,
+                                 parameters={"V_th": nb.float32(-50.0)}))
+    net.add_layer(nb.NeuronLayer.poisson_rate(npoi, rate_bias_hz=200.0, rate_gain_hz_per_current=0.0))
+    src = rng.integers(n, n + npoi, size=8000).astype(np.int32)
+    tgt = rng.integers(0, n, size=8000).astype(np.int32)
+    typ = (rng.random(8000) < 0.25).astype(np.int32)
+    net.connect(nb.Connection(src, tgt, synapse_type=typ, weight=rng.uniform(0.01, 0.06, 8000).astype(np.float32),
+                              delay=rng.integers(1, 6, 8000).astype(np.int32)))
+    cfg = nb.SimulationConfig(steps=1500, timestep=0.5)
+    sim = nb.Simulation(net, cfg, semantics="dense")
+    sim.run()
+    o = _oracle(net, cfg, semantics=1)
+    o.run(cfg.steps)
+    assert len(sim.spike_raster()[0]) > 0
+    assert _raster_equal(sim.spike_raster(), _oracle_raster(o, net))
+    for f in (0, 1, 2, 3):
+        assert np.array_equal(sim.state_field(f), o.state(f).astype(np.float32)), f
+
+
 def test_run_calls_compose():
     net, cfg = workloads.plain_lif(n=400, steps=1000)
     a = nb.Simulation(net, cfg)
