@@ -460,17 +460,9 @@ def main() -> None:
         flush.fill_(1.0)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    if world > 1:
-        import torch.distributed as dist
+    from neuronbridge_gb300.replicas import aggregate
 
-        t = torch.tensor([tot_dev, tot_wall], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e = torch.tensor([tot_ev], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(e, op=dist.ReduceOp.SUM)
-        tot_dev, tot_wall = float(t[0]), float(t[1])
-        tot_ev_all = float(e[0])
-    else:
-        tot_ev_all = tot_ev
+    (tot_dev, tot_wall), (tot_ev_all,) = aggregate([tot_dev, tot_wall], [tot_ev], device=f"cuda:{local}")
     if rank != 0:
         return
 

@@ -175,6 +175,9 @@ nbg_status nbg_num_events(nbg_engine *e, int64_t *n);
 /* Weights and STDP state in original connection order. */
 nbg_status nbg_get_weights(nbg_engine *e, float *w, float *apre, float *apost, int32_t *last);
 nbg_status nbg_set_weight(nbg_engine *e, int64_t conn, float w);
+/* All weights at once, original connection order (weight snapshot load,
+ * the reference's Simulation::LoadWeight, Simulation.h:363). */
+nbg_status nbg_set_weights(nbg_engine *e, const float *w);
 
 /* Set neuron `id`'s external current to `value` at the start of step t
  * (before that step's arrivals), as a delay-d current connection from an

@@ -93,6 +93,7 @@ _SIGNATURES = {
     "nbg_num_events": (ctypes.c_int, [ctypes.c_void_p, _i64p]),
     "nbg_get_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p, _f32p, _f32p, _i32p]),
     "nbg_set_weight": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_float]),
+    "nbg_set_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p]),
     "nbg_set_current_at": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
     "nbg_set_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _i32p]),
     "nbg_num_trace_rows": (ctypes.c_int, [ctypes.c_void_p, _i64p]),

@@ -1696,6 +1696,17 @@ nbg_status nbg_set_weight(nbg_engine *e, int64_t conn, float w) {
     return NBG_OK;
 }
 
+nbg_status nbg_set_weights(nbg_engine *e, const float *w) {
+    if (!e || (!w && e->S > 0)) return fail(NBG_ERR_INVALID, "null argument");
+    for (int64_t s = 0; s < e->S; ++s)
+        if (!std::isfinite(w[s])) return fail(NBG_ERR_INVALID, "weight %lld is not finite", (long long)s);
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    for (int64_t s = 0; s < e->S; ++s) e->init_w[e->orig_pos[s]] = w[s];
+    if (e->S > 0) NBG_CUDA(cudaMemcpy(e->w.p, e->init_w.data(), e->S * sizeof(float), cudaMemcpyHostToDevice));
+    return NBG_OK;
+}
+
 nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value) {
     if (!e) return fail(NBG_ERR_INVALID, "null engine");
     if (id < 0 || id >= e->N) return fail(NBG_ERR_INVALID, "neuron id %d out of range", id);

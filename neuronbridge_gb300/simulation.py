@@ -261,6 +261,34 @@ class Simulation:
             _lib.check(self.lib.nbg_set_current_at(self._h, int(t), int(i), float(v)))
         return self
 
+    def save_weights(self, path) -> "Simulation":
+        """Write all weights as an NPGR_WEIGHT_SNAPSHOT v1 file (the reference's
+        Simulation.save_weights)."""
+        from .weightio import write_snapshot
+
+        try:
+            write_snapshot(path, self.weights()["weight"], max(0, self.next_time - 1))
+        except ValueError as exc:
+            raise RuntimeError(f"SaveWeightToFile failed: {exc}") from None
+        return self
+
+    def load_weights(self, path) -> "Simulation":
+        """Read an NPGR_WEIGHT_SNAPSHOT v1 file and replace all weights; the
+        main block must have one weight per connection (all-or-nothing)."""
+        from .weightio import read_snapshot
+
+        try:
+            snap = read_snapshot(path)
+            w = np.ascontiguousarray(snap["main"], np.float32)
+            if len(w) != len(self.description.source):
+                raise ValueError("main weight block count does not match simulation network")
+            if snap["dense"]:
+                raise ValueError("dense weight block count does not match simulation dense subnetworks")
+        except ValueError as exc:
+            raise RuntimeError(f"LoadWeight failed: {exc}") from None
+        _lib.check(self.lib.nbg_set_weights(self._h, _p(w, ctypes.c_float)))
+        return self
+
     # ----------------------------------------------------------------- traces
     def set_trace(self, neuron_ids) -> "Simulation":
         ids = np.ascontiguousarray(neuron_ids, np.int32)

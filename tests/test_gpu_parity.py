@@ -220,3 +220,42 @@ def test_weight_get_set_by_original_index():
     assert s.get_connection_weight(5) == np.float32(1.25)
     with pytest.raises(nb.NbgError):
         s.set_connection_weight(10**9, 1.0)
+
+
+def test_weight_snapshot_round_trip(tmp_path, oracle_lib):
+    """The reference's weight_roundtrip case (set 0.75, save, set 0.15, load
+    gives 0.75), then a learned STDP network: its snapshot loaded into a fresh
+    simulation reproduces every weight bit, and the loaded simulation keeps
+    running exactly as the oracle does from the same weights."""
+    import oracle
+
+    net, cfg = workloads.plain_lif(n=100, steps=10)
+    s = nb.Simulation(net, cfg)
+    path = tmp_path / "weights.dat"
+    s.set_connection_weight(0, 0.75).save_weights(path)
+    s.set_connection_weight(0, 0.15).load_weights(path)
+    assert s.get_connection_weight(0) == np.float32(0.75)
+    assert path.read_text().startswith("NPGR_WEIGHT_SNAPSHOT 1\ntime_step ")
+
+    net, cfg = workloads.izhikevich_stdp(n=1000, in_degree=50)
+    a = nb.Simulation(net, cfg, seed=2)
+    a.run(1000)
+    learned = a.weights()["weight"]
+    assert not np.array_equal(learned, net.to_native().weight)
+    a.save_weights(path)
+
+    b = nb.Simulation(net, cfg, seed=2)
+    b.load_weights(path)
+    assert np.array_equal(b.weights()["weight"], learned)
+    b.run(200)
+    desc = net.to_native()
+    desc.weight = learned.copy()
+    ref = oracle.OracleNet(desc.flat(cfg.timestep, seed=2))
+    ref.run(200)
+    assert np.array_equal(b.weights()["weight"], ref.weights()[0].astype(np.float32))
+    assert _raster_equal(b.spike_raster(), _oracle_raster(ref, net))
+
+    bad = tmp_path / "short.dat"
+    bad.write_text("NPGR_WEIGHT_SNAPSHOT 1\ntime_step 0\nblock main 0 1\nrle\n1 0.5\nend_block\nend\n")
+    with pytest.raises(RuntimeError, match="LoadWeight failed: main weight block count does not match"):
+        b.load_weights(bad)
