@@ -78,90 +78,200 @@ def readout_coefficients(T: int, a_out: float) -> np.ndarray:
     return ((1.0 - a_out ** (T - t)) / ((1.0 - a_out) * T)).astype(np.float32)
 
 
+def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out):
+    """Forward recurrence into caller-owned buffers: the checkpoints
+    ck_*[segment] (state entering each K-step segment), the readout
+    accumulator z and the output z W_out.  Launches only (no host sync), so it
+    runs eagerly or under CUDA graph capture alike."""
+    T, B, C = x.shape
+    N = w_rec.shape[0]
+    st = _stream()
+    v = torch.full((B, N), p.v_reset, device=x.device, dtype=torch.float32)
+    ref = torch.zeros((B, N), device=x.device, dtype=torch.int32)
+    sbuf = [torch.empty((B, N), device=x.device, dtype=torch.float32) for _ in range(2)]
+    s_prev = sbuf[1]
+    s_prev.zero_()
+    z.zero_()
+    I = torch.empty((B, N), device=x.device, dtype=torch.float32)
+    for seg, t0 in enumerate(range(0, T, K)):
+        t1 = min(T, t0 + K)
+        ck_v[seg].copy_(v)
+        ck_ref[seg].copy_(ref)
+        ck_s[seg].copy_(s_prev)
+        xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
+        for t in range(t0, t1):
+            torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
+            s = sbuf[t & 1]
+            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
+                                                float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
+            s_prev = s
+    torch.mm(z, w_out, out=out)
+
+
+def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref, ck_s, p, K, coef):
+    """Adjoint sweep: replay each segment from its checkpoint (recording
+    u_t, s_t, m_t, v_{t-1}), then run the fused adjoint step in reverse time.
+    Returns the gradients of (W_in, W_rec, W_out, alpha, theta).  Launches
+    only, like the forward body."""
+    T, B, C = x.shape
+    N = w_rec.shape[0]
+    st = _stream()
+    g_read = gy @ w_out.t()
+    g_w_out = z.t() @ gy
+    g_w_in = torch.zeros_like(w_in)
+    g_w_rec = torch.zeros_like(w_rec)
+    lam_v = torch.zeros((B, N), device=x.device, dtype=torch.float32)
+    g_theta = torch.zeros((B, N), device=x.device, dtype=torch.float32)
+    g_alpha = torch.zeros((B, N), device=x.device, dtype=torch.float32)
+    g_ext = torch.empty((B, N), device=x.device, dtype=torch.float32)
+    I = torch.empty((B, N), device=x.device, dtype=torch.float32)
+    L_max = min(K, T)
+    U = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
+    S = torch.empty((L_max + 1, B, N), device=x.device, dtype=torch.float32)  # S[0] = s_{t0-1}
+    M = torch.empty((L_max, B, N), device=x.device, dtype=torch.uint8)
+    VP = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
+    dI = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
+    dI_next = torch.empty((B, N), device=x.device, dtype=torch.float32)
+    have_next = False
+    segments = list(enumerate(range(0, T, K)))
+    for seg, t0 in reversed(segments):
+        t1 = min(T, t0 + K)
+        L = t1 - t0
+        v, ref = ck_v[seg].clone(), ck_ref[seg].clone()
+        S[0].copy_(ck_s[seg])
+        xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
+        for k in range(L):
+            torch.addmm(xi[k], S[k], w_rec, out=I)
+            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
+                                                _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
+                                                ctypes.byref(p), B, N, st))
+        for k in reversed(range(L)):
+            t = t0 + k
+            ge = None
+            if have_next:
+                torch.mm(dI_next if k == L - 1 else dI[k + 1], w_rec.t(), out=g_ext)
+                ge = g_ext
+            _lib.check(lib.nbg_lif_adjoint_step(_ptr(ge), _ptr(g_read), float(coef[t]), _ptr(U[k]),
+                                                _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]), _ptr(lam_v),
+                                                _ptr(dI[k]), _ptr(g_theta), _ptr(g_alpha), _ptr(alpha),
+                                                _ptr(theta), ctypes.byref(p), B, N, st))
+            have_next = True
+        g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
+        g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
+        dI_next.copy_(dI[0])
+    return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0)
+
+
+class _GraphPlan:
+    """The forward and the backward of one shape, each captured once as a CUDA
+    graph over static buffers and replayed on later calls (the recurrence is
+    thousands of small launches; replay removes their host cost).  Inputs are
+    copied into the static buffers before a replay and results cloned out, so
+    callers never alias graph memory.  Keyed by shape, checkpoint interval,
+    readout coefficients, LIF parameters and the parameters' storage; in-place
+    optimiser updates keep the storage, so one plan serves a training run."""
+
+    def __init__(self, x, w_in, w_rec, w_out, alpha, theta, p, K, coef):
+        T, B, C = x.shape
+        N = w_rec.shape[0]
+        nseg = (T + K - 1) // K
+        dev = x.device
+        self.params = (w_in, w_rec, w_out, alpha, theta)
+        self.p, self.K, self.coef = p, K, coef
+        self.x = torch.empty_like(x)
+        self.ck_v = torch.empty((nseg, B, N), device=dev, dtype=torch.float32)
+        self.ck_ref = torch.empty((nseg, B, N), device=dev, dtype=torch.int32)
+        self.ck_s = torch.empty((nseg, B, N), device=dev, dtype=torch.float32)
+        self.z = torch.empty((B, N), device=dev, dtype=torch.float32)
+        self.out = torch.empty((B, w_out.shape[1]), device=dev, dtype=torch.float32)
+        self.gy = torch.empty((B, w_out.shape[1]), device=dev, dtype=torch.float32)
+        self.fwd = self.bwd = None
+        self.grads = None
+        self.owner = None  # the forward whose x and checkpoints the buffers hold
+
+    @staticmethod
+    def _capture(fn):
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):  # warm-up: cuBLAS handles and workspaces exist before capture
+            out = fn()
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            out = fn()
+        return g, out
+
+    def forward(self, x):
+        lib = _bind()
+        self.x.copy_(x)
+        if self.fwd is None:
+            w_in, w_rec, w_out, alpha, theta = self.params
+            self.fwd, _ = self._capture(lambda: _forward_body(
+                lib, self.x, w_in, w_rec, w_out, alpha, theta, self.p, self.K, self.coef, self.ck_v, self.ck_ref,
+                self.ck_s, self.z, self.out))
+        self.fwd.replay()
+        self.owner = object()
+        return self.owner
+
+    def backward(self, owner, gy, x, saved):
+        lib = _bind()
+        if owner is not self.owner:  # another forward ran since: restore this one's inputs
+            self.x.copy_(x)
+            self.ck_v.copy_(saved[0])
+            self.ck_ref.copy_(saved[1])
+            self.ck_s.copy_(saved[2])
+            self.z.copy_(saved[3])
+            self.owner = owner
+        self.gy.copy_(gy)
+        if self.bwd is None:
+            w_in, w_rec, w_out, alpha, theta = self.params
+            self.bwd, self.grads = self._capture(lambda: _backward_body(
+                lib, self.gy, self.x, w_in, w_rec, w_out, alpha, theta, self.z, self.ck_v, self.ck_ref, self.ck_s,
+                self.p, self.K, self.coef))
+        self.bwd.replay()
+        return tuple(g.clone() for g in self.grads)
+
+
 class _Recurrence(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, w_in, w_rec, w_out, alpha, theta, cfg):
         lib = _bind()
         T, B, C = x.shape
         N = w_rec.shape[0]
-        p = cfg["params"]
         K = cfg["checkpoint"]
-        coef = cfg["coef"]
-        st = _stream()
-        v = torch.full((B, N), p.v_reset, device=x.device, dtype=torch.float32)
-        ref = torch.zeros((B, N), device=x.device, dtype=torch.int32)
-        s_prev = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-        z = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-        ckpts = []
-        sbuf = [torch.empty((B, N), device=x.device, dtype=torch.float32) for _ in range(2)]
-        I = torch.empty((B, N), device=x.device, dtype=torch.float32)
-        for t0 in range(0, T, K):
-            t1 = min(T, t0 + K)
-            ckpts.append((t0, t1, v.clone(), ref.clone(), s_prev.clone()))
-            xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
-            for t in range(t0, t1):
-                torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
-                s = sbuf[t & 1]
-                _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
-                                                    float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N,
-                                                    st))
-                s_prev = s
-        ctx.save_for_backward(x, w_in, w_rec, w_out, alpha, theta, z)
+        nseg = (T + K - 1) // K
+        plan = cfg.get("plan")
         ctx.cfg = cfg
-        ctx.ckpts = ckpts
-        return z @ w_out
+        if plan is not None:
+            ctx.owner = plan.forward(x)
+            z = plan.z.clone()
+            saved = (plan.ck_v.clone(), plan.ck_ref.clone(), plan.ck_s.clone()) if cfg["needs_grad"] else ()
+            ctx.ck = saved
+            ctx.save_for_backward(x, w_in, w_rec, w_out, alpha, theta, z)
+            return plan.out.clone()
+        ck_v = torch.empty((nseg, B, N), device=x.device, dtype=torch.float32)
+        ck_ref = torch.empty((nseg, B, N), device=x.device, dtype=torch.int32)
+        ck_s = torch.empty((nseg, B, N), device=x.device, dtype=torch.float32)
+        z = torch.empty((B, N), device=x.device, dtype=torch.float32)
+        out = torch.empty((B, w_out.shape[1]), device=x.device, dtype=torch.float32)
+        _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, cfg["params"], K, cfg["coef"], ck_v, ck_ref, ck_s,
+                      z, out)
+        ctx.ck = (ck_v, ck_ref, ck_s)
+        ctx.save_for_backward(x, w_in, w_rec, w_out, alpha, theta, z)
+        return out
 
     @staticmethod
     def backward(ctx, gy):
-        lib = _bind()
         x, w_in, w_rec, w_out, alpha, theta, z = ctx.saved_tensors
         cfg = ctx.cfg
-        p = cfg["params"]
-        coef = cfg["coef"]
-        T, B, C = x.shape
-        N = w_rec.shape[0]
-        st = _stream()
         gy = gy.contiguous()
-        g_read = (gy @ w_out.t()).contiguous()
-        g_w_out = z.t() @ gy
-        g_w_in = torch.zeros_like(w_in)
-        g_w_rec = torch.zeros_like(w_rec)
-        lam_v = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-        g_theta = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-        g_alpha = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-        g_ext = torch.empty((B, N), device=x.device, dtype=torch.float32)
-        I = torch.empty((B, N), device=x.device, dtype=torch.float32)
-        dI_next = None
-        for (t0, t1, v0, ref0, s0) in reversed(ctx.ckpts):
-            L = t1 - t0
-            v, ref = v0.clone(), ref0.clone()
-            U = torch.empty((L, B, N), device=x.device, dtype=torch.float32)
-            S = torch.empty((L + 1, B, N), device=x.device, dtype=torch.float32)  # S[0] = s_{t0-1}
-            M = torch.empty((L, B, N), device=x.device, dtype=torch.uint8)
-            VP = torch.empty((L, B, N), device=x.device, dtype=torch.float32)
-            S[0].copy_(s0)
-            xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
-            for k in range(L):  # recompute the segment, recording what the adjoint needs
-                torch.addmm(xi[k], S[k], w_rec, out=I)
-                _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
-                                                    _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
-                                                    ctypes.byref(p), B, N, st))
-            dI = torch.empty((L, B, N), device=x.device, dtype=torch.float32)
-            for k in reversed(range(L)):
-                t = t0 + k
-                ge = None
-                if dI_next is not None:
-                    torch.mm(dI_next, w_rec.t(), out=g_ext)
-                    ge = g_ext
-                _lib.check(lib.nbg_lif_adjoint_step(_ptr(ge), _ptr(g_read), float(coef[t]), _ptr(U[k]),
-                                                    _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]), _ptr(lam_v),
-                                                    _ptr(dI[k]), _ptr(g_theta), _ptr(g_alpha), _ptr(alpha),
-                                                    _ptr(theta), ctypes.byref(p), B, N, st))
-                dI_next = dI[k]
-            g_w_rec += S[:L].reshape(-1, N).t() @ dI.reshape(-1, N)
-            g_w_in += x[t0:t1].reshape(-1, C).t() @ dI.reshape(-1, N)
-            dI_next = dI[0].clone()
-        return None, g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), None
+        plan = cfg.get("plan")
+        if plan is not None:
+            grads = plan.backward(ctx.owner, gy, x, ctx.ck + (z,))
+        else:
+            grads = _backward_body(_bind(), gy, x, w_in, w_rec, w_out, alpha, theta, z, *ctx.ck, cfg["params"],
+                                   cfg["checkpoint"], cfg["coef"])
+        return (None, *grads, None)
 
 
 class RecurrentLIF(torch.nn.Module):
@@ -171,7 +281,7 @@ class RecurrentLIF(torch.nn.Module):
     def __init__(self, n_in: int = 256, n_rec: int = 1024, n_out: int = 10, *, dt: float = 1.0, tau: float = 20.0,
                  v_rest: float = -65.0, v_reset: float = -65.0, v_th: float = -50.0, t_ref_ms: float = 2.0,
                  tau_out: float = 20.0, slope: float = 10.0, smooth: bool = False, checkpoint: int = 100,
-                 weight_scale: float = 1.0, seed: int = 5, device: str = "cuda"):
+                 weight_scale: float = 1.0, seed: int = 5, device: str = "cuda", use_graphs: bool = True):
         super().__init__()
         g = torch.Generator().manual_seed(seed)
         init = lambda *shape: (torch.randn(*shape, generator=g, dtype=torch.float64) * weight_scale /
@@ -183,12 +293,26 @@ class RecurrentLIF(torch.nn.Module):
         self.theta = torch.nn.Parameter(torch.full((n_rec,), v_th, device=device))
         self.params = GradParams(v_rest, v_reset, slope, int(round(t_ref_ms / dt)), int(bool(smooth)))
         self.dt, self.tau_out, self.checkpoint = dt, tau_out, int(checkpoint)
+        self.use_graphs = bool(use_graphs)
+        self._plans = {}
 
     def forward(self, x: torch.Tensor) -> torch.Tensor:
         T = x.shape[0]
         a_out = math.exp(-self.dt / self.tau_out)
-        cfg = {"params": self.params, "checkpoint": self.checkpoint, "coef": readout_coefficients(T, a_out)}
-        return _Recurrence.apply(x.contiguous(), self.w_in, self.w_rec, self.w_out, self.alpha, self.theta, cfg)
+        coef = readout_coefficients(T, a_out)
+        x = x.contiguous()
+        cfg = {"params": self.params, "checkpoint": self.checkpoint, "coef": coef,
+               "needs_grad": torch.is_grad_enabled() and any(q.requires_grad for q in self.parameters())}
+        if self.use_graphs:
+            key = (tuple(x.shape), str(x.device), self.checkpoint, coef.tobytes(), bytes(self.params),
+                   tuple(q.data_ptr() for q in self.parameters()))
+            plan = self._plans.get(key)
+            if plan is None:
+                self._plans.clear()
+                plan = self._plans[key] = _GraphPlan(x, self.w_in, self.w_rec, self.w_out, self.alpha, self.theta,
+                                                     self.params, self.checkpoint, coef)
+            cfg["plan"] = plan
+        return _Recurrence.apply(x, self.w_in, self.w_rec, self.w_out, self.alpha, self.theta, cfg)
 
 
 def reference_forward(x, w_in, w_rec, w_out, alpha, theta, *, v_rest=-65.0, v_reset=-65.0, slope=10.0, t_ref=2,
