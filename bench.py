@@ -444,7 +444,7 @@ def main() -> None:
         torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    tot_ev = tot_wall = tot_dev = tot_upd = tot_prop = 0.0
+    tot_ev = tot_wall = tot_dev = tot_upd = 0.0
     tot_spk = tot_post = 0
     launches = 0
     for _ in range(args.steps):
@@ -453,7 +453,6 @@ def main() -> None:
         tot_wall += wall
         tot_dev += prof["device_ms"] / 1e3
         tot_upd += prof["update_kernel_ms"] / 1e3
-        tot_prop += prof["propagate_kernel_ms"] / 1e3
         tot_spk += nspk
         tot_post += int(fan[new_ids].sum())
         launches += prof["kernel_launches"]
@@ -488,15 +487,14 @@ def main() -> None:
                    else "single"},
         "neuron_steps_per_s": n * sim_steps * world / tot_dev,
         "spikes_per_s_simulated": tot_spk / (sim_steps * 1e-4) / n,
-        "roofline": {"bound": "hbm", "kernel": "k_update (drain + RK4 + STDP)",
+        "roofline": {"bound": "hbm", "kernel": "k_update (drain + RK4 + STDP + spike propagation)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
                      "traffic": KUPDATE_TRAFFIC_BYTES if args.sim_steps % 10 == 0 else None,
                      "traffic_unit": "bytes per launch (ncu, cold L2)",
-                     "algorithmic_bytes_per_launch": upd_bytes / max(1, launches // 2),
+                     "algorithmic_bytes_per_launch": upd_bytes / max(1, launches),
                      "update_ms_share": tot_upd / tot_dev if tot_dev else None,
-                     "propagate_ms_share": tot_prop / tot_dev if tot_dev else None,
-                     "avg_update_launch_us": 1e6 * tot_upd / max(1, launches // 2)},
+                     "avg_update_launch_us": 1e6 * tot_upd / max(1, launches)},
         "e2e": {"value": tot_ev_all / tot_wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 4 + 8 + 4,
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

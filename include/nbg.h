@@ -58,8 +58,19 @@ enum {
     NBG_MODEL_LIF_VJ = 0,   /* TimeDrivenLIF_Voltage_jump[_GPU] */
     NBG_MODEL_IZH_COND = 1, /* TimeDrivenIzhikevic_[I_]Exponential_Decay[_GPU] */
     NBG_MODEL_IZH_RK4 = 2,  /* IzhikevichCurrentRK4: current pulses, noise, RK4 */
-    NBG_MODEL_POISSON = 3   /* PoissonRate[_GPU] */
+    NBG_MODEL_POISSON = 3,  /* PoissonRate[_GPU] */
+    /* Event-driven input layers (InputSpikeNeuronModel,
+     * InputCurrentNeuronModel; python/src/neuronbridge/model.py:162-185): no
+     * dynamics, never fire by themselves.  Their neurons are the sources of
+     * nbg_add_external_spikes / nbg_add_external_currents. */
+    NBG_MODEL_INPUT_SPIKE = 4,
+    NBG_MODEL_INPUT_CURRENT = 5
 };
+
+/* Synapse types: 0 excitatory, 1 inhibitory (spike synapses), 3 current
+ * synapse (carries the latched current of its input-current source, see
+ * nbg_add_external_currents; never a learning rule). */
+enum { NBG_SYN_EXC = 0, NBG_SYN_INH = 1, NBG_SYN_CURRENT = 3 };
 
 /* Semantics profile: LEGACY_CPU is the parity target (strict '>' LIF
  * threshold, refractory-gated arrivals); DENSE follows the reference's dense
@@ -78,7 +89,8 @@ enum { NBG_SEM_LEGACY_CPU = 0, NBG_SEM_DENSE = 1 };
  *            f[11] I_ext
  *  IZH_RK4:  f[0] a, f[1] b, f[2] c, f[3] d, f[4] v0, f[5] V_th,
  *            f[6] noise sigma, f[7] I_bias
- *  POISSON:  f[0] rate_bias_hz, f[1] rate_gain_hz_per_current, f[2] I_ext */
+ *  POISSON:  f[0] rate_bias_hz, f[1] rate_gain_hz_per_current, f[2] I_ext
+ *  INPUT_SPIKE, INPUT_CURRENT: no parameters */
 typedef struct {
     int model;
     int count;
@@ -97,7 +109,8 @@ typedef struct {
  * assigned layer by layer), then connections as parallel arrays in original
  * connection order (the reference's ConnectionDescription,
  * Network/inc/NetworkConstructStructure.h:18-74).  type 0 = excitatory,
- * 1 = inhibitory; delay in steps (>= 1); rule = index into rules or -1. */
+ * 1 = inhibitory, 3 = current; delay in steps (>= 1); rule = index into
+ * rules or -1 (always -1 for a current synapse). */
 typedef struct {
     int n_layers;
     const nbg_layer_desc *layers;
@@ -185,6 +198,33 @@ nbg_status nbg_set_weights(nbg_engine *e, const float *w);
  * target's total current, e.g. TimeDrivenLIF_Voltage_jump.cpp:117-124;
  * PROPOGATEDCURRENT outranks PROPOGATEDSPIKE, Event.h:10). */
 nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value);
+
+/* External spikes (Simulation::AddExternalSpikeActivity, Simulation.h:256;
+ * ArrayInputSpikeDriver.cpp:15-24; InputSpike.cpp:12-29): neuron ids[k]
+ * emits a spike at step times[k].  It is recorded in the raster (if its layer
+ * is an output) and delivered over its out-going spike synapses at
+ * times[k] + delay, with the pre-synaptic learning hook, exactly like a spike
+ * of the update; the neuron's own state and the post-synaptic hook are not
+ * touched.  The delivery is fused into the propagation kernel of the block
+ * that contains times[k] (no per-step host work).  Sources must belong to an
+ * NBG_MODEL_INPUT_SPIKE layer (such a neuron never fires by itself, so one
+ * spike per step is all it can carry); a (time, neuron) pair given twice, or
+ * a time before nbg_next_time, is rejected.  Events after the current call
+ * stay pending for later calls; nbg_reset drops them. */
+nbg_status nbg_add_external_spikes(nbg_engine *e, int64_t n, const int32_t *times, const int32_t *ids);
+
+/* External currents (Simulation::AddExternalCurrentActivity, Simulation.h:258;
+ * ArrayInputCurrentDriver.cpp:12-19; InputCurrent.cpp:13-24;
+ * PropogatedCurrent.cpp:13-24): input-current neuron ids[k] sends currents[k]
+ * at step times[k] over each of its current synapses (type 3).  At
+ * times[k] + delay the synapse latches the value, and its target's external
+ * current becomes the float sum of the latched values of all its current
+ * synapses (in the target's synapse order: source, delay, connection index),
+ * as CurrentSynapse::GetTotalInputCurrentPerNeuron does before
+ * ProcessCurrent stores it (TimeDrivenLIF_Voltage_jump.cpp:117-124).  Applied
+ * at the start of that step, after any nbg_set_current_at value for it. */
+nbg_status nbg_add_external_currents(nbg_engine *e, int64_t n, const int32_t *times, const int32_t *ids,
+                                     const float *currents);
 /* A PoissonRate layer without incoming synapses is a generator: its spikes
  * are a pure function of (local index, step), so targets evaluate them inline
  * instead of through the delay ring.  Timed currents into generator neurons

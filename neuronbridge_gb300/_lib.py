@@ -19,6 +19,9 @@ MODEL_LIF_VJ = 0
 MODEL_IZH_COND = 1
 MODEL_IZH_RK4 = 2
 MODEL_POISSON = 3
+MODEL_INPUT_SPIKE = 4
+MODEL_INPUT_CURRENT = 5
+SYN_CURRENT = 3
 
 SEM_LEGACY_CPU = 0
 SEM_DENSE = 1
@@ -94,6 +97,8 @@ _SIGNATURES = {
     "nbg_get_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p, _f32p, _f32p, _i32p]),
     "nbg_set_weight": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_float]),
     "nbg_set_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p]),
+    "nbg_add_external_spikes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _i32p, _i32p]),
+    "nbg_add_external_currents": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _i32p, _i32p, _f32p]),
     "nbg_set_current_at": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
     "nbg_set_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _i32p]),
     "nbg_num_trace_rows": (ctypes.c_int, [ctypes.c_void_p, _i64p]),

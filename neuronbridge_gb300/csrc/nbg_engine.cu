@@ -1,6 +1,6 @@
 // nbg_engine.cu -- GB300 (sm_103a) step engine for NeuronBridge's time-driven
-// spiking networks: network compile on the host, two kernels per block of
-// steps on the device, C ABI in include/nbg.h.
+// spiking networks: network compile on the host, one kernel launch per block
+// of steps on the device, C ABI in include/nbg.h.
 //
 // Execution model (owner computes by target neuron):
 //   * Every synapse has a bit in a per-step "arrival mask" ring:
@@ -11,14 +11,17 @@
 //     arrivals in ascending CSC order (the canonical order of the oracle),
 //     runs the pre-synaptic STDP hook of each plastic arrival, integrates the
 //     neuron, and on a spike runs the post-synaptic STDP pass over its own
-//     CSC list.  Spikes are compacted per step with a warp ballot.
-//   * k_propagate: for every spike of the block, every out-synapse (CSR by
-//     source) sets its bit in slot (t + delay) % D with atomicOr.  OR is
-//     commutative, so the mask -- and therefore every later sum -- does not
-//     depend on the order in which threads run: results are bit-exact and
-//     reproducible without floating-point atomics.
+//     CSC list and propagates the spike: the warp strides over the spiking
+//     neuron's out-synapses (CSR by source) and sets each one's bit in slot
+//     (t + delay) % D with a fire-and-forget atomicOr.  OR is commutative, so
+//     the mask -- and therefore every later sum -- does not depend on the
+//     order in which threads run: results are bit-exact and reproducible
+//     without floating-point atomics.
 //   * Temporal blocking: a spike at t reaches its targets at t + d >= t + dmin,
-//     so B = dmin steps can be advanced per target with no global exchange.
+//     so B <= dmin steps can be advanced per target with no global exchange.
+//     The ring has D = dmax + Bmax slots, so a mark made during a block
+//     (for a step >= the block's end) never lands in a slot the block is
+//     still draining: the marks of a launch are read only by later launches.
 //
 // Reference counterparts (paths inside the reference project):
 //   LIF update     .../NeuralModel/src/TimeDriven/TimeDrivenLIF_Voltage_jump.cpp:49-113
@@ -45,6 +48,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include "nbg.h"
@@ -114,9 +118,8 @@ struct NetDev {
     // in-synapses from generator layers, per target, sorted by CSC rank
     const int *gen_ptr, *gen_pos, *gen_src;
     const unsigned short *gen_delay;
-    int *blk_spk, *blk_cnt;
-    int *out_ids, *out_cnt;
-    long long *cursor;
+    int *out_ids, *out_t; // raster of output-layer spikes (unordered; sorted on the host)
+    unsigned int *cursor;
     long long out_cap;
     int *err;
     int *run_t0;
@@ -128,6 +131,9 @@ struct NetDev {
     unsigned long long *ev_cursor;
     long long ev_cap;
     unsigned long long *n_events;
+    // external spikes of the current run call: ext_ids[ext_ptr[k] .. ext_ptr[k+1])
+    // spike at call step k (null until the first nbg_add_external_spikes)
+    const int *ext_ptr, *ext_ids;
 };
 
 __device__ __forceinline__ float hash_uniform01(int neuron_index, int time_step) {
@@ -312,6 +318,9 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, N
             r.ginh = r.ginh + w;
         }
         break;
+    case NBG_MODEL_INPUT_SPIKE:
+    case NBG_MODEL_INPUT_CURRENT: // event-driven inputs: ProcessSpike has no effect
+        break;
     default: // IZH_RK4 current pulse, POISSON rate increment
         acc_a = acc_a + (type ? -w : w);
         break;
@@ -479,6 +488,9 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
         }
         return false;
     }
+    case NBG_MODEL_INPUT_SPIKE:
+    case NBG_MODEL_INPUT_CURRENT: // no time-driven dynamics
+        return false;
     default: { // POISSON
         float rate = M.p[0] + acc_a + M.p[1] * r.iext;
         rate = rate > 0.0f ? rate : 0.0f;
@@ -558,28 +570,47 @@ __device__ __forceinline__ void summary_clear_range(unsigned int *srow, int woff
     }
 }
 
-// Launch parameters of one block of steps: B steps starting toff steps
-// after the run's first step; par = the block's parity (its spike counters);
-// bprev = the previous block's step count (0 for the first block of a run).
-__global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B, int toff, int par,
-                                                  int bprev) {
+// Mark the out-synapses [q0, q1) of a spike at step t (the calling lanes
+// stride over them): bit of the synapse in slot (t + delay) % D and the
+// summary bit of its word.  No return values are used, so the atomics are
+// fire-and-forget reductions.
+__device__ __forceinline__ void mark_out(const NetDev &n, int q, int q1, unsigned int t) {
+#pragma unroll 4
+    for (; q < q1; q += 32) {
+        const unsigned int bit = n.out_bit[q];
+        const unsigned int slot = (t + n.out_delay[q]) % (unsigned int)n.D;
+        const unsigned int wd = bit >> 5;
+        atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
+        atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+    }
+}
+
+// One block of B steps starting toff steps after the run call's first step.
+__global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B, int toff) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = j < n.N;
     const int lane = threadIdx.x & 31;
     const int run_t0 = *n.run_t0;
     const int T0 = run_t0 + toff;
-    int *cnt = n.blk_cnt + par * kMaxBlockSteps;
-    if (j == 0 && bprev > 0) { // publish the previous block's raster length
-        const int *prev = n.blk_cnt + (par ^ 1) * kMaxBlockSteps;
-        long long add = 0;
-        for (int b = 0; b < bprev; ++b) add += prev[b];
-        *n.cursor += add;
+    // external spikes of the block's steps (InputSpike::ProcessEvent): one
+    // warp per spike marks its out-synapses like a spike of the update (their
+    // arrivals fall after this block, so marking first is safe); the raster
+    // entries are added on the host, which holds the list
+    if (n.ext_ptr) {
+        const int e0 = n.ext_ptr[toff], e1 = n.ext_ptr[toff + B];
+        const int nwarps = (gridDim.x * blockDim.x) >> 5;
+        for (int g = j >> 5; g < e1 - e0; g += nwarps) {
+            const int x = e0 + g;
+            int b = 0;
+            while (b + 1 < B && n.ext_ptr[toff + b + 1] <= x) ++b;
+            const int src = n.ext_ids[x];
+            mark_out(n, n.out_ptr[src] + lane, n.out_ptr[src + 1], (unsigned int)(T0 + b));
+        }
     }
 
     Model L;
     NeuronRegs r;
     int base = 0, end = 0, woff = 0, nw = 0, tslot = -1, g0 = 0, g1 = 0;
-    bool listed = false;
     if (active) {
         L = load_model(n.layers[n.pop[j]]);
         r.v = n.v[j];
@@ -595,8 +626,6 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
         if (n.trace_slot) tslot = n.trace_slot[j];
         g0 = n.gen_ptr[j];
         g1 = n.gen_ptr[j + 1];
-        // compacted if its spikes are recorded or must be propagated
-        listed = L.record || n.out_ptr[j + 1] > n.out_ptr[j];
     }
     GenIn gin[kGenCached];
 #pragma unroll
@@ -635,6 +664,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
             if ((sb_cur >> k) & 1u) w_cur[k] = r0[k];
     }
     unsigned long long delivered = 0;
+    unsigned int spk_steps = 0u; // bit b: this neuron spiked at step T0 + b
     for (int b = 0; b < B; ++b) {
         const int t = T0 + b;
         bool spk = false;
@@ -716,14 +746,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
             spk = update_neuron(n, L, r, acc_a, acc_b, nz[b], j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
         }
-        const unsigned int bal = __ballot_sync(0xffffffffu, spk && listed);
-        if (bal) {
-            const int leader = __ffs(bal) - 1;
-            int pos = 0;
-            if (lane == leader) pos = atomicAdd(&cnt[b], __popc(bal));
-            pos = __shfl_sync(0xffffffffu, pos, leader);
-            if (spk && listed) n.blk_spk[(size_t)b * n.N + pos + __popc(bal & ((1u << lane) - 1u))] = j;
-        }
+        if (spk) spk_steps |= 1u << b;
         // post-synaptic STDP (STDP::ApplyPostSynaticSpike) of every spiking
         // lane, the warp striding over that neuron's in-synapses
         unsigned int sbal = __ballot_sync(0xffffffffu, spk && end > base);
@@ -742,59 +765,59 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
         n.ginh[j] = r.ginh;
         n.last[j] = r.last;
     }
+    // The block's spikes leave the warp after its last step: nothing in this
+    // launch reads their marks (arrivals fall at or after T0 + B, and the
+    // ring never aliases this block's slots), so the loads they need overlap
+    // with other warps' steps instead of stalling every step.
+    // Raster: output-layer spikes, one cursor reservation per warp.
+    {
+        const int nrec = (active && L.record) ? __popc(spk_steps) : 0;
+        int incl = nrec;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total > 0) {
+            unsigned int pos = 0;
+            if (lane == 31) pos = atomicAdd(n.cursor, (unsigned int)total);
+            pos = __shfl_sync(0xffffffffu, pos, 31) + (unsigned int)(incl - nrec);
+            if (nrec > 0) {
+                if (pos + (unsigned int)nrec <= (unsigned int)n.out_cap) {
+                    for (unsigned int m = spk_steps; m; m &= m - 1u, ++pos) {
+                        n.out_ids[pos] = j;
+                        n.out_t[pos] = T0 + __ffs(m) - 1;
+                    }
+                } else {
+                    atomicOr(n.err, kErrOverflow);
+                }
+            }
+        }
+    }
+    // Propagation: the warp strides over each spiking lane's out-synapses,
+    // loading each synapse once and marking it for every step it spiked in.
+    unsigned int pbal = __ballot_sync(0xffffffffu, spk_steps != 0u);
+    while (pbal) {
+        const int l = __ffs(pbal) - 1;
+        pbal &= pbal - 1u;
+        const int jl = j - lane + l;
+        const unsigned int steps = __shfl_sync(0xffffffffu, spk_steps, l);
+        const int q1 = n.out_ptr[jl + 1];
+#pragma unroll 2
+        for (int q = n.out_ptr[jl] + lane; q < q1; q += 32) {
+            const unsigned int bit = n.out_bit[q];
+            const unsigned int dl = n.out_delay[q];
+            const unsigned int wd = bit >> 5;
+            for (unsigned int m = steps; m; m &= m - 1u) {
+                const unsigned int slot = ((unsigned int)T0 + (unsigned int)(__ffs(m) - 1) + dl) % (unsigned int)n.D;
+                atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
+                atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+            }
+        }
+    }
     // warp-aggregated delivered-event count
     for (int o = 16; o > 0; o >>= 1) delivered += __shfl_down_sync(0xffffffffu, delivered, o);
     if (lane == 0 && delivered) atomicAdd(n.n_events, delivered);
-}
-
-// Propagate the spikes of the last B steps: one warp per spike, lanes over its
-// out-synapses; also appends the spikes to the run's raster in step order at
-// the cursor the next update launch advances.  CTA 0 records the per-step
-// counts and clears the other parity's counters for the next block.
-__global__ void __launch_bounds__(256, 2) k_propagate(const __grid_constant__ NetDev n, int B, int toff, int par) {
-    __shared__ int pre[kMaxBlockSteps + 1];
-    const int T0 = *n.run_t0 + toff;
-    const int *cnt = n.blk_cnt + par * kMaxBlockSteps;
-    if (threadIdx.x == 0) {
-        int s = 0;
-        for (int b = 0; b < B; ++b) {
-            pre[b] = s;
-            s += cnt[b];
-        }
-        pre[B] = s;
-    }
-    __syncthreads();
-    const int total = pre[B];
-    const long long cur = *n.cursor;
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int g = gw; g < total; g += nwarps) {
-        int b = 0;
-        while (b + 1 < B && pre[b + 1] <= g) ++b;
-        const int src = n.blk_spk[(size_t)b * n.N + (g - pre[b])];
-        const unsigned int t = (unsigned int)(T0 + b);
-        if (lane == 0) {
-            // non-output neurons keep their slot as -1 (dropped on the host)
-            if (cur + g < n.out_cap) n.out_ids[cur + g] = n.layers[n.pop[src]].record ? src : -1;
-            else atomicOr(n.err, kErrOverflow);
-        }
-        const int q0 = n.out_ptr[src], q1 = n.out_ptr[src + 1];
-        // fire-and-forget reductions (no return value is used): the loads of
-        // later iterations do not wait on earlier atomics
-#pragma unroll 4
-        for (int q = q0 + lane; q < q1; q += 32) {
-            const unsigned int bit = n.out_bit[q];
-            const unsigned int slot = (t + n.out_delay[q]) % (unsigned int)n.D;
-            const unsigned int wd = bit >> 5;
-            atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
-            atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
-        }
-    }
-    if (blockIdx.x == 0 && (int)threadIdx.x < kMaxBlockSteps) {
-        if ((int)threadIdx.x < B) n.out_cnt[toff + threadIdx.x] = cnt[threadIdx.x];
-        n.blk_cnt[(par ^ 1) * kMaxBlockSteps + threadIdx.x] = 0;
-    }
 }
 
 // ------------------------------------------------------------------ host side
@@ -831,12 +854,12 @@ struct nbg_engine {
     DevBuf<float> v, u, gexc, ginh, iext, w, wmax, apre, apost, dtab, rule_a, trace, ev_w;
     DevBuf<int> gen_ptr, gen_pos, gen_src;
     DevBuf<unsigned short> gen_delay;
-    DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, blk_spk, blk_cnt, out_ids, out_cnt, err, run_t0,
+    DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, out_ids, out_t, err, run_t0,
         trace_slot, ev_t, ev_pos;
     DevBuf<unsigned int> mask, wsum, out_bit;
     int Ws = 1;
     DevBuf<unsigned short> out_delay;
-    DevBuf<long long> cursor;
+    DevBuf<unsigned int> cursor;
     DevBuf<unsigned long long> ev_cursor, n_events;
     int dtab_len = 0;
     bool dtab_complete = false; // table reached exact zero: longer gaps decay to 0
@@ -852,6 +875,24 @@ struct nbg_engine {
         float value;
     };
     std::vector<CurrentEvent> currents; // pending, sorted by time
+    // external spikes: pending (time, neuron) pairs, and the device list of
+    // the current call
+    std::vector<std::pair<int, int>> ext_pending;
+    std::unordered_set<uint64_t> ext_keys;
+    std::vector<int> ext_ptr_h, ext_ids_h;
+    DevBuf<int> ext_ptr_d, ext_ids_d;
+    // current synapses (type 3): per source the out-going ones (target,
+    // delay, latch slot); latch slots are grouped by target in CSC order
+    std::vector<int> cur_out_ptr, cur_out_tgt, cur_out_delay, cur_out_slot;
+    std::vector<int> cur_tgt_ptr; // target j: latch slots [cur_tgt_ptr[j], cur_tgt_ptr[j+1])
+    std::vector<float> cur_latch;
+    struct LatchEvent {
+        int t, slot;
+        float value;
+        int64_t seq;
+    };
+    std::vector<LatchEvent> latches; // pending
+    int64_t latch_seq = 0;
     std::vector<int32_t> log_t;
     std::vector<int64_t> log_conn;
     std::vector<float> log_w;
@@ -861,7 +902,6 @@ struct nbg_engine {
     cudaGraphExec_t graph = nullptr;
     int graph_blocks = 0, graph_tail = 0, graph_B = 0, graph_threads = 0;
     NetDev graph_nd{}; // kernel arguments baked into the graph
-    int prop_grid = 0;
     double last_ms = 0.0, last_upd_ms = 0.0, last_prop_ms = 0.0;
     int64_t last_launches = 0;
     bool kernel_timing = false;
@@ -906,10 +946,8 @@ struct nbg_engine {
         n.gen_pos = gen_pos.p;
         n.gen_src = gen_src.p;
         n.gen_delay = gen_delay.p;
-        n.blk_spk = blk_spk.p;
-        n.blk_cnt = blk_cnt.p;
         n.out_ids = out_ids.p;
-        n.out_cnt = out_cnt.p;
+        n.out_t = out_t.p;
         n.cursor = cursor.p;
         n.out_cap = (long long)out_ids.n;
         n.err = err.p;
@@ -923,6 +961,8 @@ struct nbg_engine {
         n.ev_cursor = ev_cursor.p;
         n.ev_cap = ev_cap;
         n.n_events = n_events.p;
+        n.ext_ptr = ext_ptr_d.p;
+        n.ext_ids = ext_ids_d.p;
         return n;
     }
 };
@@ -987,7 +1027,6 @@ nbg_status reset_state(nbg_engine *e) {
     }
     NBG_CUDA(e->mask.zero());
     NBG_CUDA(e->wsum.zero());
-    NBG_CUDA(e->blk_cnt.zero());
     NBG_CUDA(e->err.zero());
     NBG_CUDA(e->cursor.zero());
     NBG_CUDA(e->ev_cursor.zero());
@@ -1002,15 +1041,19 @@ nbg_status reset_state(nbg_engine *e) {
     e->log_conn.clear();
     e->log_w.clear();
     e->currents.clear();
+    e->ext_pending.clear();
+    e->ext_keys.clear();
+    e->latches.clear();
+    std::fill(e->cur_latch.begin(), e->cur_latch.end(), 0.0f);
     return NBG_OK;
 }
 
 constexpr int kLaunchChunk = 64; // direct launches between timing harvests
 
-// Grow the pool of event triples used to bracket the launches.
+// Grow the pool of event pairs used to bracket the launches.
 nbg_status ensure_timing_events(nbg_engine *e, int blocks) {
     if (!e->kernel_timing) return NBG_OK;
-    while ((int)e->tev.size() < 3 * blocks) {
+    while ((int)e->tev.size() < 2 * blocks) {
         cudaEvent_t ev;
         NBG_CUDA(cudaEventCreate(&ev));
         e->tev.push_back(ev);
@@ -1019,30 +1062,25 @@ nbg_status ensure_timing_events(nbg_engine *e, int blocks) {
 }
 
 // Launch one block of B steps.  With kernel timing, `slot` selects the event
-// triple bracketing the two kernels.
+// pair bracketing the launch.
 // Inside stream capture an event record must be "external" to become an
 // event-record node of the graph (a plain record is only a dependency).
-void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int par, int bprev, int slot,
-                  bool capturing = false) {
+void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int slot, bool capturing = false) {
     const int grid = (e->N + e->threads - 1) / e->threads;
     const unsigned int flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 0], e->stream, flags);
-    k_update<<<grid, e->threads, 0, e->stream>>>(nd, B, toff, par, bprev);
-    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 1], e->stream, flags);
-    k_propagate<<<e->prop_grid, 256, 0, e->stream>>>(nd, B, toff, par);
-    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[3 * slot + 2], e->stream, flags);
+    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 0], e->stream, flags);
+    k_update<<<grid, e->threads, 0, e->stream>>>(nd, B, toff);
+    if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 1], e->stream, flags);
 }
 
-// Sum the bracketed kernel durations of `blocks` event triples.
+// Sum the bracketed kernel durations of `blocks` event pairs.
 nbg_status harvest_timing(nbg_engine *e, int blocks) {
     if (!e->kernel_timing || blocks == 0) return NBG_OK;
-    NBG_CUDA(cudaEventSynchronize(e->tev[3 * (blocks - 1) + 2]));
+    NBG_CUDA(cudaEventSynchronize(e->tev[2 * (blocks - 1) + 1]));
     for (int k = 0; k < blocks; ++k) {
-        float a = 0.0f, b = 0.0f;
-        NBG_CUDA(cudaEventElapsedTime(&a, e->tev[3 * k + 0], e->tev[3 * k + 1]));
-        NBG_CUDA(cudaEventElapsedTime(&b, e->tev[3 * k + 1], e->tev[3 * k + 2]));
+        float a = 0.0f;
+        NBG_CUDA(cudaEventElapsedTime(&a, e->tev[2 * k + 0], e->tev[2 * k + 1]));
         e->last_upd_ms += a;
-        e->last_prop_ms += b;
     }
     return NBG_OK;
 }
@@ -1090,7 +1128,8 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     int64_t total = 0;
     for (int l = 0; l < d->n_layers; ++l) {
         const nbg_layer_desc &ld = d->layers[l];
-        if (ld.model < 0 || ld.model > 3) return fail(NBG_ERR_INVALID, "layer %d: unknown model %d", l, ld.model);
+        if (ld.model < 0 || ld.model > NBG_MODEL_INPUT_CURRENT)
+            return fail(NBG_ERR_INVALID, "layer %d: unknown model %d", l, ld.model);
         if (ld.count <= 0) return fail(NBG_ERR_INVALID, "layer %d: count must be positive", l);
         total += ld.count;
     }
@@ -1165,8 +1204,10 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
                 e->init_u[i] = ld.f[1] * ld.f[4];
                 e->init_iext[i] = ld.f[7];
                 break;
-            default:
+            case NBG_MODEL_POISSON:
                 e->init_iext[i] = ld.f[2];
+                break;
+            default: // input layers: no state
                 break;
             }
         }
@@ -1185,17 +1226,24 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
             return bail(fail(NBG_ERR_INVALID, "connection %lld: neuron id out of range", (long long)s));
         if (d->delay[s] < 1 || d->delay[s] > 65535)
             return bail(fail(NBG_ERR_INVALID, "connection %lld: delay must be in 1..65535 steps", (long long)s));
-        if (d->type[s] != 0 && d->type[s] != 1)
-            return bail(fail(NBG_ERR_UNSUPPORTED, "connection %lld: synapse type %d not supported (0 exc, 1 inh)",
+        if (d->type[s] != NBG_SYN_EXC && d->type[s] != NBG_SYN_INH && d->type[s] != NBG_SYN_CURRENT)
+            return bail(fail(NBG_ERR_UNSUPPORTED,
+                             "connection %lld: synapse type %d not supported (0 exc, 1 inh, 3 current)",
                              (long long)s, d->type[s]));
+        if ((d->type[s] == NBG_SYN_CURRENT) != (e->layers[pop[a]].model == NBG_MODEL_INPUT_CURRENT))
+            return bail(fail(NBG_ERR_UNSUPPORTED,
+                             "connection %lld: input-current neurons connect through current synapses (type 3) "
+                             "and only they do", (long long)s));
+        if (d->type[s] == NBG_SYN_CURRENT && d->rule[s] != -1)
+            return bail(fail(NBG_ERR_UNSUPPORTED, "connection %lld: a current synapse cannot learn", (long long)s));
         if (d->rule[s] < -1 || d->rule[s] >= d->n_rules)
             return bail(fail(NBG_ERR_INVALID, "connection %lld: learning rule %d out of range", (long long)s,
                              d->rule[s]));
         if (!std::isfinite(d->weight[s]) || !std::isfinite(d->max_weight[s]))
             return bail(fail(NBG_ERR_INVALID, "connection %lld: weight must be finite", (long long)s));
         indeg[b + 1]++;
-        if (d->type[s] == 0) e->layers[pop[b]].has_exc = 1;
-        else e->layers[pop[b]].has_inh = 1;
+        if (d->type[s] == NBG_SYN_EXC) e->layers[pop[b]].has_exc = 1;
+        else if (d->type[s] == NBG_SYN_INH) e->layers[pop[b]].has_inh = 1;
     }
     // generator layers: PoissonRate layers without incoming synapses
     {
@@ -1205,7 +1253,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
             e->layers[l].generator = e->layers[l].model == NBG_MODEL_POISSON && layer_in[l] == 0;
     }
     for (int64_t s = 0; s < S; ++s) {
-        if (e->layers[pop[d->source[s]]].generator) continue;
+        if (e->layers[pop[d->source[s]]].generator || d->type[s] == NBG_SYN_CURRENT) continue;
         e->dmin = std::min(e->dmin, d->delay[s]);
         e->dmax = std::max(e->dmax, d->delay[s]);
     }
@@ -1233,7 +1281,9 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     std::vector<int> woff((size_t)e->N + 1, 0);
     for (int j = 0; j < e->N; ++j) woff[j + 1] = woff[j] + (cptr[j + 1] - cptr[j] + 31) / 32;
     e->Wt = std::max(woff[e->N], 1);
-    e->D = e->dmax + 1;
+    // ring slots: every delay plus the longest block, so that no mark made
+    // inside a block aliases a slot the block drains
+    e->D = e->dmax + std::min(e->dmin, kMaxBlockSteps);
     e->pop_host = pop;
     std::vector<float> w((size_t)S), wmax((size_t)S);
     std::vector<unsigned char> meta((size_t)S);
@@ -1249,11 +1299,47 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     e->plastic = false;
     for (int64_t s = 0; s < S && !e->plastic; ++s) e->plastic = d->rule[s] >= 0;
 
-    // ---- CSR by source over (mask bit, delay); generator sources excluded
+    // ---- current synapses: latch slots by target (CSC order), out-lists by source
+    {
+        std::vector<unsigned char> is_cur((size_t)S, 0);
+        e->cur_tgt_ptr.assign((size_t)e->N + 1, 0);
+        e->cur_out_ptr.assign((size_t)e->N + 1, 0);
+        for (int j = 0; j < e->N; ++j)
+            for (int p = cptr[j]; p < cptr[j + 1]; ++p)
+                if (d->type[e->csc_orig[p]] == NBG_SYN_CURRENT) {
+                    is_cur[p] = 1;
+                    e->cur_tgt_ptr[j + 1]++;
+                    e->cur_out_ptr[src_of[p] + 1]++;
+                }
+        for (int i = 0; i < e->N; ++i) {
+            e->cur_tgt_ptr[i + 1] += e->cur_tgt_ptr[i];
+            e->cur_out_ptr[i + 1] += e->cur_out_ptr[i];
+        }
+        const int nc = e->cur_tgt_ptr[e->N];
+        e->cur_latch.assign((size_t)nc, 0.0f);
+        e->cur_out_tgt.assign((size_t)nc, 0);
+        e->cur_out_delay.assign((size_t)nc, 0);
+        e->cur_out_slot.assign((size_t)nc, 0);
+        std::vector<int> fill(e->cur_out_ptr.begin(), e->cur_out_ptr.end() - 1);
+        int slot = 0;
+        for (int j = 0; j < e->N; ++j)
+            for (int p = cptr[j]; p < cptr[j + 1]; ++p)
+                if (is_cur[p]) {
+                    const int q = fill[src_of[p]]++;
+                    e->cur_out_tgt[q] = j;
+                    e->cur_out_delay[q] = d->delay[e->csc_orig[p]];
+                    e->cur_out_slot[q] = slot++;
+                }
+    }
+
+    // ---- CSR by source over (mask bit, delay); generator sources and
+    // current synapses excluded
+    auto spike_syn = [&](int p) { return d->type[e->csc_orig[p]] != NBG_SYN_CURRENT; };
     std::vector<int> optr((size_t)e->N + 1, 0);
     std::vector<int> gptr((size_t)e->N + 1, 0);
     for (int j = 0; j < e->N; ++j)
         for (int p = cptr[j]; p < cptr[j + 1]; ++p) {
+            if (!spike_syn(p)) continue;
             if (e->layers[pop[src_of[p]]].generator) gptr[j + 1]++;
             else optr[src_of[p] + 1]++;
         }
@@ -1270,6 +1356,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
         int gq = 0;
         for (int j = 0; j < e->N; ++j)
             for (int p = cptr[j]; p < cptr[j + 1]; ++p) {
+                if (!spike_syn(p)) continue;
                 const unsigned short dl = (unsigned short)d->delay[e->csc_orig[p]];
                 if (e->layers[pop[src_of[p]]].generator) {
                     gpos[gq] = p - cptr[j]; // ascending within j: CSC order
@@ -1329,8 +1416,6 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(e->gen_pos.upload(gpos), "gen_pos");
     chk(e->gen_src.upload(gsrc), "gen_src");
     chk(e->gen_delay.upload(gdelay), "gen_delay");
-    chk(e->blk_spk.alloc((size_t)kMaxBlockSteps * N), "block spike lists");
-    chk(e->blk_cnt.alloc(2 * kMaxBlockSteps), "block counts");
     chk(e->err.alloc(1), "err");
     chk(e->run_t0.alloc(1), "run_t0");
     chk(e->cursor.alloc(1), "cursor");
@@ -1354,11 +1439,6 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     if (st == NBG_OK) st = ensure_decay_table(e, 4096);
     if (st == NBG_OK) st = reset_state(e);
     if (st != NBG_OK) return bail(st);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
-    // propagate CTAs: one per SM for small networks, up to 8 per SM for large
-    // ones (more spikes per block than warps otherwise)
-    e->prop_grid = std::max(std::max(1, sms), std::min(std::max(1, sms) * 8, e->N / 4096));
     e->spike_capacity = opt.spike_capacity;
     *out = e;
     return NBG_OK;
@@ -1396,15 +1476,48 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     // raster capacity for this call
     int64_t cap = e->spike_capacity > 0 ? e->spike_capacity
                                         : std::min<int64_t>((int64_t)e->N * count, (int64_t)1 << 26);
-    cap = std::max<int64_t>(cap, 1);
-    if ((int64_t)e->out_ids.n < cap) NBG_CUDA(e->out_ids.alloc((size_t)cap));
-    if ((int64_t)e->out_cnt.n < count) NBG_CUDA(e->out_cnt.alloc((size_t)count));
+    cap = std::min<int64_t>(std::max<int64_t>(cap, 1), 0x7FFFFFFF); // 32-bit device cursor
+    if ((int64_t)e->out_ids.n < cap) {
+        NBG_CUDA(e->out_ids.alloc((size_t)cap));
+        NBG_CUDA(e->out_t.alloc((size_t)cap));
+    }
     const int ntr = (int)e->trace_ids.size();
     if (ntr > 0 && (int64_t)e->trace.n < (int64_t)count * ntr) NBG_CUDA(e->trace.alloc((size_t)count * ntr));
     const int t0 = e->next_t;
+    // external spikes of this call: per-step lists on the device
+    std::vector<std::pair<int, int>> ext_due;
+    if (!e->ext_pending.empty()) {
+        std::vector<std::pair<int, int>> later;
+        for (const auto &x : e->ext_pending) {
+            if (x.first < t0 + count) {
+                ext_due.push_back(x);
+                e->ext_keys.erase(((uint64_t)(uint32_t)x.first << 32) | (uint32_t)x.second);
+            } else {
+                later.push_back(x);
+            }
+        }
+        e->ext_pending.swap(later);
+        std::sort(ext_due.begin(), ext_due.end());
+    }
+    if (!ext_due.empty() || e->ext_ptr_d.p) {
+        if ((int64_t)e->ext_ptr_d.n < count + 1) NBG_CUDA(e->ext_ptr_d.alloc((size_t)count + 1));
+        if (e->ext_ids_d.n < std::max<size_t>(ext_due.size(), 1))
+            NBG_CUDA(e->ext_ids_d.alloc(std::max<size_t>(ext_due.size(), 1)));
+        e->ext_ptr_h.assign((size_t)count + 1, 0);
+        e->ext_ids_h.resize(ext_due.size());
+        for (size_t k = 0; k < ext_due.size(); ++k) {
+            e->ext_ptr_h[(size_t)(ext_due[k].first - t0) + 1]++;
+            e->ext_ids_h[k] = ext_due[k].second;
+        }
+        for (int k = 0; k < count; ++k) e->ext_ptr_h[(size_t)k + 1] += e->ext_ptr_h[(size_t)k];
+        NBG_CUDA(cudaMemcpyAsync(e->ext_ptr_d.p, e->ext_ptr_h.data(), ((size_t)count + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, e->stream));
+        if (!ext_due.empty())
+            NBG_CUDA(cudaMemcpyAsync(e->ext_ids_d.p, e->ext_ids_h.data(), ext_due.size() * sizeof(int),
+                                     cudaMemcpyHostToDevice, e->stream));
+    }
     NBG_CUDA(cudaMemcpyAsync(e->run_t0.p, &t0, sizeof(int), cudaMemcpyHostToDevice, e->stream));
-    NBG_CUDA(cudaMemsetAsync(e->cursor.p, 0, sizeof(long long), e->stream));
-    NBG_CUDA(cudaMemsetAsync(e->blk_cnt.p, 0, 2 * kMaxBlockSteps * sizeof(int), e->stream));
+    NBG_CUDA(cudaMemsetAsync(e->cursor.p, 0, sizeof(unsigned int), e->stream));
     NBG_CUDA(cudaMemsetAsync(e->err.p, 0, sizeof(int), e->stream));
     const NetDev nd = e->dev();
 
@@ -1423,6 +1536,36 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         }
         e->currents.swap(later);
     }
+    // latched currents due in this call, in time order: after all latches of a
+    // step, each touched target's total (float sum over its slots in order)
+    if (!e->latches.empty()) {
+        std::vector<nbg_engine::LatchEvent> now, later;
+        for (const auto &x : e->latches) (x.t < t0 + count ? now : later).push_back(x);
+        e->latches.swap(later);
+        std::sort(now.begin(), now.end(), [](const nbg_engine::LatchEvent &a, const nbg_engine::LatchEvent &b) {
+            return a.t != b.t ? a.t < b.t : a.seq < b.seq;
+        });
+        std::vector<int> touched;
+        for (size_t k = 0; k < now.size();) {
+            const int t = now[k].t;
+            touched.clear();
+            for (; k < now.size() && now[k].t == t; ++k) {
+                e->cur_latch[(size_t)now[k].slot] = now[k].value;
+                const int j = (int)(std::upper_bound(e->cur_tgt_ptr.begin(), e->cur_tgt_ptr.end(), now[k].slot) -
+                                    e->cur_tgt_ptr.begin()) - 1;
+                touched.push_back(j);
+            }
+            std::sort(touched.begin(), touched.end());
+            touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+            for (int j : touched) {
+                float total = 0.0f;
+                for (int q = e->cur_tgt_ptr[j]; q < e->cur_tgt_ptr[j + 1]; ++q) total += e->cur_latch[(size_t)q];
+                due.push_back({t, j, total});
+            }
+        }
+        std::stable_sort(due.begin(), due.end(), [](const nbg_engine::CurrentEvent &a,
+                                                    const nbg_engine::CurrentEvent &b) { return a.t < b.t; });
+    }
     const int t_end = t0 + count;
     if (e->use_graph && due.empty()) {
         // the whole call as one graph: nfull blocks of B steps and a tail block
@@ -1438,8 +1581,8 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
             }
             cudaGraph_t g;
             NBG_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < nfull; ++k) launch_block(e, nd, B, k * B, k & 1, k ? B : 0, k, true);
-            if (tail) launch_block(e, nd, tail, nfull * B, nfull & 1, nfull ? B : 0, nfull, true);
+            for (int k = 0; k < nfull; ++k) launch_block(e, nd, B, k * B, k, true);
+            if (tail) launch_block(e, nd, tail, nfull * B, nfull, true);
             NBG_CUDA(cudaStreamEndCapture(e->stream, &g));
             cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
             cudaGraphDestroy(g);
@@ -1453,14 +1596,13 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         NBG_CUDA(cudaGraphLaunch(e->graph, e->stream));
         nbg_status hs = harvest_timing(e, nblocks);
         if (hs != NBG_OK) return hs;
-        launches += 2LL * nblocks;
+        launches += nblocks;
     } else {
         // direct launches, split at timed current injections
         nbg_status ps = ensure_timing_events(e, kLaunchChunk);
         if (ps != NBG_OK) return ps;
         int t = t0;
         size_t ci = 0;
-        int nlaunch = 0, bprev = 0;
         while (t < t_end) {
             while (ci < due.size() && due[ci].t == t) {
                 NBG_CUDA(cudaMemcpyAsync(e->iext.p + due[ci].id, &due[ci].value, sizeof(float),
@@ -1474,10 +1616,8 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
             int slot = 0;
             for (int k = 0; k < nblocks; ++k) {
                 const int bk = std::min(B, seg - k * B);
-                launch_block(e, nd, bk, t + k * B - t0, nlaunch & 1, bprev, slot++);
-                bprev = bk;
-                ++nlaunch;
-                launches += 2;
+                launch_block(e, nd, bk, t + k * B - t0, slot++);
+                ++launches;
                 if (slot == kLaunchChunk) {
                     nbg_status hs = harvest_timing(e, slot);
                     if (hs != NBG_OK) return hs;
@@ -1504,26 +1644,33 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     if (errv & kErrEventLog) return fail(NBG_ERR_OVERFLOW, "delivered-event log capacity exceeded");
     if (errv & kErrOverflow)
         return fail(NBG_ERR_OVERFLOW, "spike raster capacity (%lld) exceeded in this run call", (long long)cap);
-    // raster: per-step counts and ids, sorted by id within a step
-    std::vector<int> cnt((size_t)count);
-    NBG_CUDA(cudaMemcpy(cnt.data(), e->out_cnt.p, count * sizeof(int), cudaMemcpyDeviceToHost));
-    long long nspk = 0;
-    for (int c : cnt) nspk += c;
-    const size_t base = e->spk_id.size();
-    e->spk_id.resize(base + (size_t)nspk);
-    e->spk_t.resize(base + (size_t)nspk);
-    if (nspk > 0)
-        NBG_CUDA(cudaMemcpy(e->spk_id.data() + base, e->out_ids.p, nspk * sizeof(int), cudaMemcpyDeviceToHost));
-    size_t in = base, out = base;
-    for (int k = 0; k < count; ++k) {
-        const size_t step_begin = out;
-        for (int q = 0; q < cnt[k]; ++q, ++in)
-            if (e->spk_id[in] >= 0) e->spk_id[out++] = e->spk_id[in];
-        std::sort(e->spk_id.begin() + step_begin, e->spk_id.begin() + out);
-        std::fill(e->spk_t.begin() + step_begin, e->spk_t.begin() + out, t0 + k);
+    // raster: the device's unordered (step, id) entries plus the external
+    // spikes of output neurons, bucketed by step and sorted by id within it
+    unsigned int ndev = 0;
+    NBG_CUDA(cudaMemcpy(&ndev, e->cursor.p, sizeof(ndev), cudaMemcpyDeviceToHost));
+    std::vector<int> ids((size_t)ndev), ts((size_t)ndev);
+    if (ndev > 0) {
+        NBG_CUDA(cudaMemcpy(ids.data(), e->out_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(ts.data(), e->out_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
     }
-    e->spk_id.resize(out);
-    e->spk_t.resize(out);
+    std::vector<size_t> at((size_t)count + 1, 0);
+    for (size_t k = 0; k < (size_t)ndev; ++k) at[(size_t)(ts[k] - t0) + 1]++;
+    for (const auto &x : ext_due)
+        if (e->layers[e->pop_host[x.second]].record) at[(size_t)(x.first - t0) + 1]++;
+    for (int k = 0; k < count; ++k) at[(size_t)k + 1] += at[(size_t)k];
+    const size_t base = e->spk_id.size();
+    e->spk_id.resize(base + at[(size_t)count]);
+    e->spk_t.resize(base + at[(size_t)count]);
+    {
+        std::vector<size_t> fill(at.begin(), at.end() - 1);
+        for (size_t k = 0; k < (size_t)ndev; ++k) e->spk_id[base + fill[(size_t)(ts[k] - t0)]++] = ids[k];
+        for (const auto &x : ext_due)
+            if (e->layers[e->pop_host[x.second]].record) e->spk_id[base + fill[(size_t)(x.first - t0)]++] = x.second;
+    }
+    for (int k = 0; k < count; ++k) {
+        std::sort(e->spk_id.begin() + base + at[(size_t)k], e->spk_id.begin() + base + at[(size_t)k + 1]);
+        std::fill(e->spk_t.begin() + base + at[(size_t)k], e->spk_t.begin() + base + at[(size_t)k + 1], t0 + k);
+    }
     if (ntr > 0) {
         const size_t rb = e->trace_rows.size();
         e->trace_rows.resize(rb + (size_t)count * ntr);
@@ -1720,6 +1867,62 @@ nbg_status nbg_set_current_at(nbg_engine *e, int t, int id, float value) {
                                    return a.t < b.t;
                                });
     e->currents.insert(it, c);
+    return NBG_OK;
+}
+
+nbg_status nbg_add_external_spikes(nbg_engine *e, int64_t n, const int32_t *times, const int32_t *ids) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (n < 0 || (n > 0 && (!times || !ids))) return fail(NBG_ERR_INVALID, "bad external spike arrays");
+    std::vector<uint64_t> keys((size_t)n);
+    for (int64_t k = 0; k < n; ++k) {
+        const int t = times[k], id = ids[k];
+        if (id < 0 || id >= e->N) return fail(NBG_ERR_INVALID, "external spike %lld: neuron id %d out of range",
+                                              (long long)k, id);
+        if (t < e->next_t)
+            return fail(NBG_ERR_INVALID, "external spike %lld: time %d is in the past (next step %d)", (long long)k,
+                        t, e->next_t);
+        if (e->layers[e->pop_host[id]].model != NBG_MODEL_INPUT_SPIKE)
+            return fail(NBG_ERR_UNSUPPORTED, "external spike %lld: neuron %d is not an input-spike neuron",
+                        (long long)k, id);
+        keys[(size_t)k] = ((uint64_t)(uint32_t)t << 32) | (uint32_t)id;
+    }
+    std::unordered_set<uint64_t> seen;
+    for (int64_t k = 0; k < n; ++k)
+        if (e->ext_keys.count(keys[(size_t)k]) || !seen.insert(keys[(size_t)k]).second)
+            return fail(NBG_ERR_UNSUPPORTED, "external spike %lld: neuron %d already spikes at step %d",
+                        (long long)k, ids[k], times[k]);
+    for (int64_t k = 0; k < n; ++k) {
+        e->ext_keys.insert(keys[(size_t)k]);
+        e->ext_pending.emplace_back(times[k], ids[k]);
+    }
+    return NBG_OK;
+}
+
+nbg_status nbg_add_external_currents(nbg_engine *e, int64_t n, const int32_t *times, const int32_t *ids,
+                                     const float *currents) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (n < 0 || (n > 0 && (!times || !ids || !currents))) return fail(NBG_ERR_INVALID, "bad external current arrays");
+    for (int64_t k = 0; k < n; ++k) {
+        if (ids[k] < 0 || ids[k] >= e->N)
+            return fail(NBG_ERR_INVALID, "external current %lld: neuron id %d out of range", (long long)k, ids[k]);
+        if (times[k] < e->next_t)
+            return fail(NBG_ERR_INVALID, "external current %lld: time %d is in the past (next step %d)",
+                        (long long)k, times[k], e->next_t);
+        if (e->layers[e->pop_host[ids[k]]].model != NBG_MODEL_INPUT_CURRENT)
+            return fail(NBG_ERR_UNSUPPORTED, "external current %lld: neuron %d is not an input-current neuron",
+                        (long long)k, ids[k]);
+        if (!std::isfinite(currents[k]))
+            return fail(NBG_ERR_INVALID, "external current %lld: value must be finite", (long long)k);
+        if ((int64_t)times[k] + 65535 > 0x7FFFFFF0ll) return fail(NBG_ERR_INVALID, "external current time overflow");
+    }
+    for (int64_t k = 0; k < n; ++k) {
+        const int src = ids[k];
+        for (int q = e->cur_out_ptr[src]; q < e->cur_out_ptr[src + 1]; ++q) {
+            const int j = e->cur_out_tgt[q];
+            if (e->layers[e->pop_host[j]].generator) continue; // unreachable: a current input is an input
+            e->latches.push_back({times[k] + e->cur_out_delay[q], e->cur_out_slot[q], currents[k], e->latch_seq++});
+        }
+    }
     return NBG_OK;
 }
 

@@ -81,6 +81,8 @@ CATALOG = {
          "TimeDrivenIzhikevic_Exponential_Decay_GPU")),
     "PoissonRate": (_lib.MODEL_POISSON, ("PoissonRate_GPU",)),
     "IzhikevichCurrentRK4": (_lib.MODEL_IZH_RK4, ()),
+    "InputSpikeNeuronModel": (_lib.MODEL_INPUT_SPIKE, ()),
+    "InputCurrentNeuronModel": (_lib.MODEL_INPUT_CURRENT, ()),
 }
 _ALIAS = {alias: canon for canon, (_, aliases) in CATALOG.items() for alias in (canon, *aliases)}
 
@@ -106,6 +108,8 @@ _PARAMS = {
         "rate_gain_hz_per_current": ("f", 1, 1.0), "poisson_rate_gain_hz_per_current": ("f", 1, 1.0),
         "I_ext": ("f", 2, 0.0),
     },
+    _lib.MODEL_INPUT_SPIKE: {},
+    _lib.MODEL_INPUT_CURRENT: {},
 }
 
 
@@ -148,6 +152,22 @@ class NeuronLayer:
             params["poisson_rate_gain_hz_per_current"] = float32(rate_gain_hz_per_current)
         return cls("PoissonRate", count, update_timestep=update_timestep, monitored=monitored, output=output,
                    communication_input=communication_input, parameters=params)
+
+    @classmethod
+    def input_spike(cls, count: int, *, update_timestep: int = 1, monitored: bool = False, output: bool = False,
+                    communication_input: bool = False, **parameters) -> "NeuronLayer":
+        """Event-driven layer whose neurons spike only through
+        Simulation.add_external_spikes (reference model.py:162-172)."""
+        return cls("InputSpikeNeuronModel", count, update_timestep=update_timestep, monitored=monitored,
+                   output=output, communication_input=communication_input, parameters=dict(parameters))
+
+    @classmethod
+    def input_current(cls, count: int, *, update_timestep: int = 1, monitored: bool = False, output: bool = False,
+                      communication_input: bool = False, **parameters) -> "NeuronLayer":
+        """Event-driven layer whose neurons send Simulation.add_external_currents
+        over their current synapses (synapse_type=3; reference model.py:174-185)."""
+        return cls("InputCurrentNeuronModel", count, update_timestep=update_timestep, monitored=monitored,
+                   output=output, communication_input=communication_input, parameters=dict(parameters))
 
     def native_params(self) -> tuple[int, np.ndarray, np.ndarray]:
         """(model id, f[16], ip[4]) for the C ABI layer descriptor."""

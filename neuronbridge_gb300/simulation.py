@@ -250,6 +250,31 @@ class Simulation:
         _lib.check(self.lib.nbg_set_weight(self._h, int(original_connection_index), float(weight)))
         return self
 
+    def add_external_spikes(self, times, neuron_ids) -> "Simulation":
+        """Spikes of input-spike neurons at the given steps, delivered over
+        their synapses inside the device step loop (the reference's
+        Simulation.add_external_spikes)."""
+        t = np.ascontiguousarray(np.atleast_1d(times), np.int64)
+        i = np.ascontiguousarray(np.atleast_1d(neuron_ids), np.int64)
+        if t.shape != i.shape:
+            raise ValueError("external spike times and neuron_ids must have the same length")
+        t32, i32 = (np.ascontiguousarray(x, np.int32) for x in (t, i))
+        _lib.check(self.lib.nbg_add_external_spikes(self._h, len(t32), _p(t32, ctypes.c_int32),
+                                                    _p(i32, ctypes.c_int32)))
+        return self
+
+    def add_external_currents(self, times, neuron_ids, currents) -> "Simulation":
+        """Currents sent by input-current neurons at the given steps over
+        their current synapses (the reference's Simulation.add_external_currents)."""
+        t = np.ascontiguousarray(np.atleast_1d(times), np.int32)
+        i = np.ascontiguousarray(np.atleast_1d(neuron_ids), np.int32)
+        c = np.ascontiguousarray(np.atleast_1d(currents), np.float32)
+        if not (t.shape == i.shape == c.shape):
+            raise ValueError("external current times, neuron_ids, and currents must have the same length")
+        _lib.check(self.lib.nbg_add_external_currents(self._h, len(t), _p(t, ctypes.c_int32),
+                                                      _p(i, ctypes.c_int32), _p(c, ctypes.c_float)))
+        return self
+
     def set_current_at(self, times, neuron_ids, currents) -> "Simulation":
         """Set each neuron's external current at the start of the given step
         (the effect of a delay-d current connection from an input-current

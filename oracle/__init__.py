@@ -86,6 +86,8 @@ def _lib(prec: int):
             "get_events": (None, [vp, i32p, i64p, f64p]),
             "set_threads": (None, [vp, ctypes.c_int]),
             "add_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+            "add_external_spike": (None, [vp, ctypes.c_int, ctypes.c_int]),
+            "add_external_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             "dense_create": (vp, [ctypes.c_int, ctypes.c_int, f32p, f32p, i32p, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float]),
             "dense_destroy": (None, [vp]),
@@ -203,6 +205,18 @@ class OracleNet:
     def add_current(self, t: int, neuron: int, value: float) -> None:
         """Set neuron's external current to ``value`` at the start of step t."""
         self._f("add_current")(self.h, int(t), int(neuron), float(value))
+
+    def add_external_spikes(self, times, neurons) -> "OracleNet":
+        """InputSpike events: each neuron spikes at its step."""
+        for t, i in zip(np.atleast_1d(times), np.atleast_1d(neurons)):
+            self._f("add_external_spike")(self.h, int(t), int(i))
+        return self
+
+    def add_external_currents(self, times, neurons, values) -> "OracleNet":
+        """InputCurrent events sent over the neurons' current synapses."""
+        for t, i, v in zip(np.atleast_1d(times), np.atleast_1d(neurons), np.atleast_1d(values)):
+            self._f("add_external_current")(self.h, int(t), int(i), float(np.float32(v)))
+        return self
 
     def set_event_log(self, on: bool = True) -> None:
         self._f("set_event_log")(self.h, int(bool(on)))

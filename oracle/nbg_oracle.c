@@ -56,7 +56,8 @@
 #endif
 
 /* model ids and parameter slots: identical numbering to include/nbg.h */
-enum { M_LIF_VJ = 0, M_IZH_COND = 1, M_IZH_RK4 = 2, M_POISSON = 3 };
+enum { M_LIF_VJ = 0, M_IZH_COND = 1, M_IZH_RK4 = 2, M_POISSON = 3, M_INPUT_SPIKE = 4, M_INPUT_CURRENT = 5 };
+enum { SYN_CURRENT = 3 };
 enum { SEM_LEGACY = 0, SEM_DENSE = 1 };
 #define NFP 16
 #define NIP 4
@@ -121,6 +122,20 @@ typedef struct {
     vec64_t cur_t, cur_id;
     REAL *cur_v;
     int64_t cur_vcap;
+    /* external spikes (t, neuron) of input-spike neurons: InputSpike events
+     * (L/InputSpikeDriver/src/ArrayInputSpikeDriver.cpp:15-24,
+     * L/Event/src/Spike/InputSpike.cpp:12-29) */
+    vec64_t ext_t, ext_id;
+    /* external currents: one latch event (time of arrival, CSC position of the
+     * current synapse, value) per current synapse of the sending input-current
+     * neuron (L/Event/src/Current/InputCurrent.cpp:13-24,
+     * PropogatedCurrent.cpp:13-24); each synapse keeps its latched value and
+     * the target's current is the float sum over its current synapses
+     * (CurrentSynapse::GetTotalInputCurrentPerNeuron) */
+    vec64_t lat_t, lat_p;
+    REAL *lat_v;
+    int64_t lat_vcap;
+    REAL *latch; /* per CSC position (only current synapses used) */
     int threads;          /* OpenMP threads for the per-step loops (1 = serial) */
     unsigned char *fired; /* per-neuron spike flags of the current update */
     int64_t *seg;         /* target segment starts of the sorted bucket */
@@ -210,7 +225,7 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
         L->count = count[l];
         for (int k = 0; k < NFP; ++k) L->f[k] = (REAL)fparams[l * NFP + k];
         for (int k = 0; k < NIP; ++k) L->ip[k] = iparams[l * NIP + k];
-        if (L->model < 0 || L->model > 3 || L->count <= 0) {
+        if (L->model < 0 || L->model > M_INPUT_CURRENT || L->count <= 0) {
             set_err(err, errlen, "bad layer");
             ORC(destroy)(n);
             return NULL;
@@ -227,8 +242,10 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
     sortkey_t *keys = (sortkey_t *)malloc((size_t)(n_conn > 0 ? n_conn : 1) * sizeof(sortkey_t));
     int dmax = 1;
     for (int64_t s = 0; s < n_conn; ++s) {
-        if (src[s] < 0 || src[s] >= total || tgt[s] < 0 || tgt[s] >= total || delay[s] < 1 || type[s] < 0 ||
-            type[s] > 1 || (rule[s] >= n_rules)) {
+        if (src[s] < 0 || src[s] >= total || tgt[s] < 0 || tgt[s] >= total || delay[s] < 1 ||
+            !(type[s] == 0 || type[s] == 1 || type[s] == SYN_CURRENT) || (rule[s] >= n_rules) ||
+            ((type[s] == SYN_CURRENT) != (n->layers[n->layer_of[src[s]]].model == M_INPUT_CURRENT)) ||
+            (type[s] == SYN_CURRENT && rule[s] >= 0)) {
             set_err(err, errlen, "bad connection");
             free(keys);
             ORC(destroy)(n);
@@ -257,6 +274,7 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
     n->apre = (REAL *)calloc(ns, sizeof(REAL));
     n->apost = (REAL *)calloc(ns, sizeof(REAL));
     n->slast = (int *)calloc(ns, sizeof(int));
+    n->latch = (REAL *)calloc(ns, sizeof(REAL));
     for (int64_t p = 0; p < n_conn; ++p) {
         int64_t s = keys[p].idx;
         n->csc_ptr[keys[p].tgt + 1]++;
@@ -402,6 +420,12 @@ void ORC(destroy)(void *hp) {
     free(n->cur_t.v);
     free(n->cur_id.v);
     free(n->cur_v);
+    free(n->ext_t.v);
+    free(n->ext_id.v);
+    free(n->lat_t.v);
+    free(n->lat_p.v);
+    free(n->lat_v);
+    free(n->latch);
     free(n->fired);
     free(n->seg);
     free(n);
@@ -653,6 +677,8 @@ static int spiked(net_t *n, layer_t *L, int i, int t) {
     case M_LIF_VJ: return spiked_lif(n, L, i);
     case M_IZH_COND: return spiked_izh_cond(n, L, i);
     case M_IZH_RK4: return spiked_izh_rk4(n, L, i, t);
+    case M_INPUT_SPIKE:
+    case M_INPUT_CURRENT: return 0; /* event-driven: no time-driven update */
     default: return spiked_poisson(n, L, i, t);
     }
 }
@@ -661,9 +687,44 @@ static int spiked(net_t *n, layer_t *L, int i, int t) {
  * updates and the post-synaptic passes of different spiking neurons run in
  * parallel; each touches only its own neuron and synapses, so the results
  * are identical to the serial order. */
+static void schedule_spike(net_t *n, int i, int t) {
+    for (int64_t q = n->out_ptr[i]; q < n->out_ptr[i + 1]; ++q) {
+        int64_t p = n->out_pos[q];
+        if (n->csc_type[p] == SYN_CURRENT) continue; /* carries currents only */
+        vpush(&n->bucket[(t + n->csc_delay[p]) % n->ring], p);
+    }
+}
+
 static void step(net_t *n, int t) {
     for (int64_t k = 0; k < n->cur_t.n; ++k)
         if (n->cur_t.v[k] == t) n->i_ext[n->cur_id.v[k]] = n->cur_v[k];
+    /* latched external currents arriving at t (insertion order), then the
+     * total of every touched target */
+    {
+        int any = 0;
+        for (int64_t k = 0; k < n->lat_t.n; ++k)
+            if (n->lat_t.v[k] == t) {
+                n->latch[n->lat_p.v[k]] = n->lat_v[k];
+                any = 1;
+            }
+        if (any)
+            for (int64_t k = 0; k < n->lat_t.n; ++k) {
+                if (n->lat_t.v[k] != t) continue;
+                int j = n->csc_tgt[n->lat_p.v[k]];
+                float total = 0.0f;
+                for (int64_t p = n->csc_ptr[j]; p < n->csc_ptr[j + 1]; ++p)
+                    if (n->csc_type[p] == SYN_CURRENT) total += (float)n->latch[p];
+                n->i_ext[j] = (REAL)total;
+            }
+    }
+    /* external spikes at t: recorded and scheduled like a spike of the
+     * update, before it (PROPOGATEDSPIKE outranks TIMEEVENT) */
+    for (int64_t k = 0; k < n->ext_t.n; ++k)
+        if (n->ext_t.v[k] == t) {
+            int i = (int)n->ext_id.v[k];
+            vpush(&n->spk, ((int64_t)t << 32) | (int64_t)(uint32_t)i);
+            schedule_spike(n, i, t);
+        }
     /* 1. arrivals due at t, per target in CSC order */
     vec64_t *b = &n->bucket[t % n->ring];
     qsort(b->v, (size_t)b->n, sizeof(int64_t), cmp_i64);
@@ -694,10 +755,7 @@ static void step(net_t *n, int t) {
         for (int i = i0; i < i1; ++i) {
             if (!n->fired[i]) continue;
             vpush(&n->spk, ((int64_t)t << 32) | (int64_t)(uint32_t)i);
-            for (int64_t q = n->out_ptr[i]; q < n->out_ptr[i + 1]; ++q) {
-                int64_t p = n->out_pos[q];
-                vpush(&n->bucket[(t + n->csc_delay[p]) % n->ring], p);
-            }
+            schedule_spike(n, i, t);
         }
         const int64_t last = n->spk.n;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(n->threads) if (n->threads > 1 && last - first > 8)
@@ -806,6 +864,27 @@ void ORC(get_events)(void *hp, int *t, int64_t *conn, double *w) {
         t[k] = (int)n->ev_t.v[k];
         conn[k] = n->csc_orig[n->ev_pos.v[k]];
         w[k] = (double)n->ev_w[k];
+    }
+}
+
+void ORC(add_external_spike)(void *hp, int t, int id) {
+    net_t *n = (net_t *)hp;
+    vpush(&n->ext_t, t);
+    vpush(&n->ext_id, id);
+}
+
+void ORC(add_external_current)(void *hp, int t, int id, double value) {
+    net_t *n = (net_t *)hp;
+    for (int64_t q = n->out_ptr[id]; q < n->out_ptr[id + 1]; ++q) {
+        int64_t p = n->out_pos[q];
+        if (n->csc_type[p] != SYN_CURRENT) continue;
+        vpush(&n->lat_t, t + n->csc_delay[p]);
+        vpush(&n->lat_p, p);
+        if (n->lat_t.n > n->lat_vcap) {
+            n->lat_vcap = n->lat_t.cap;
+            n->lat_v = (REAL *)realloc(n->lat_v, (size_t)n->lat_vcap * sizeof(REAL));
+        }
+        n->lat_v[n->lat_t.n - 1] = (REAL)value;
     }
 }
 
