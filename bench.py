@@ -56,7 +56,7 @@ BYTES_PER_STATIC_EVENT = 12
 BYTES_PER_POST_UPDATE = 36
 # DRAM bytes (read + write) of one k_update launch of this workload (10 steps x
 # 100k neurons) from an ncu capture of that launch with a cold L2
-KUPDATE_TRAFFIC_BYTES = 56.5e6
+KUPDATE_TRAFFIC_BYTES = 80.6e6
 
 
 def _peaks():
@@ -191,10 +191,11 @@ def bench_lif(args) -> dict:
     import torch
 
     import neuronbridge_gb300 as nb
-    from neuronbridge_gb300 import workloads
+    from neuronbridge_gb300 import tuning, workloads
 
     net, cfg = workloads.plain_lif()
     sim = nb.Simulation(net, cfg, kernel_timing=True)
+    tune = tuning.autotune(sim, trial_steps=1000)  # launch shape only; resets the simulation
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         sim.run(cfg.steps)
@@ -220,7 +221,7 @@ def bench_lif(args) -> dict:
     peak, kind = _peaks()
     return _common(args, "synaptic events/s", ev / dev, "synaptic events/s", 1e3 * dev / args.steps,
                    {"workload": "plain_lif_1k", "neurons": n, "sim_steps_per_step": cfg.steps,
-                    "block_steps": sim.block_steps},
+                    "block_steps": sim.block_steps, "tuned": tune["choice"]},
                    neuron_steps_per_s=n * cfg.steps * args.steps / dev,
                    roofline={"bound": "hbm", "kernel": "k_update", "achieved": upd_bytes / upd / 1e9, "peak": peak,
                              "unit": "GB/s", "frac": upd_bytes / upd / 1e9 / peak, "peak_kind": kind,
@@ -417,11 +418,12 @@ def main() -> None:
     torch.cuda.set_device(local)
 
     import neuronbridge_gb300 as nb
-    from neuronbridge_gb300 import workloads
+    from neuronbridge_gb300 import tuning, workloads
 
     net, cfg = workloads.izhikevich_stdp()
     desc = net.to_native()
     sim = nb.Simulation(desc, cfg, device=local, seed=2, kernel_timing=True)
+    tune = tuning.autotune(sim, trial_steps=500)  # launch shape only; resets the simulation
     fan = _post_fanout(desc)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
@@ -483,6 +485,7 @@ def main() -> None:
         "config": {"workload": "izhikevich_stdp_100k", "neurons": n, "synapses": int(len(desc.source)),
                    "plastic_synapses": int(np.sum(desc.rule >= 0)), "sim_steps_per_step": args.sim_steps,
                    "dt_ms": 0.1, "integrator": "rk4", "block_steps": sim.block_steps,
+                   "tuned": tune["choice"],
                    "l2": "flushed between timed iterations (256 MiB write)", "parallelism": "replicas" if world > 1
                    else "single"},
         "neuron_steps_per_s": n * sim_steps * world / tot_dev,

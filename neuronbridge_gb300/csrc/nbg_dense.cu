@@ -248,6 +248,25 @@ struct LifParams {
 // One update of every (instance, neuron): summed arrival, refractory-gated
 // voltage jump, forward-Euler voltage-jump LIF (TimeDrivenLIF_Voltage_jump.cpp
 // :49-86), spike -> S_t (BF16 0/1 for the tensor path, bit words for FP32).
+// One neuron's update (state vv, ls in registers) given its summed arrival
+// `a`; idx = the element of the instance-major state (the drive's hash index).
+__device__ __forceinline__ bool lif_apply(const LifParams &P, float a, float &vv, int &ls, int t, int idx) {
+    if (t >= 1 && nbg_hash_uniform01(idx, t - 1) < P.drive_p) a = a + P.drive_w;
+    if (ls > P.t_ref) vv = vv + a;
+    float cur = 0.0f;
+    cur = cur + P.r * P.i_ext / P.tau;
+    const float aux = (ls > P.t_ref) ? cur + (P.v_rest - vv) / P.tau : 0.0f;
+    vv = vv + aux * P.dt;
+    ls += 1;
+    bool spk = false;
+    if (vv > P.v_th) {
+        vv = P.v_reset;
+        ls = 0;
+        spk = true;
+    }
+    return spk;
+}
+
 __global__ void __launch_bounds__(256) k_dense_lif(LifParams P, const float *__restrict__ partial, int nparts,
                                                    float *__restrict__ v, int *__restrict__ last,
                                                    __nv_bfloat16 *__restrict__ s_out, int s_blocked_layout,
@@ -258,20 +277,9 @@ __global__ void __launch_bounds__(256) k_dense_lif(LifParams P, const float *__r
     if (idx < total) {
         float a = partial[idx];
         for (int k = 1; k < nparts; ++k) a = a + partial[(size_t)k * total + idx];
-        if (t >= 1 && nbg_hash_uniform01(idx, t - 1) < P.drive_p) a = a + P.drive_w;
         float vv = v[idx];
         int ls = last[idx];
-        if (ls > P.t_ref) vv = vv + a;
-        float cur = 0.0f;
-        cur = cur + P.r * P.i_ext / P.tau;
-        const float aux = (ls > P.t_ref) ? cur + (P.v_rest - vv) / P.tau : 0.0f;
-        vv = vv + aux * P.dt;
-        ls += 1;
-        if (vv > P.v_th) {
-            vv = P.v_reset;
-            ls = 0;
-            spk = true;
-        }
+        spk = lif_apply(P, a, vv, ls, t, idx);
         v[idx] = vv;
         last[idx] = ls;
         if (s_out) {
@@ -287,6 +295,34 @@ __global__ void __launch_bounds__(256) k_dense_lif(LifParams P, const float *__r
     }
 }
 
+// The step's neuron update fused into the tcgen05 delivery: the same update
+// as k_dense_lif for the elements of the tile a CTA completes, with their
+// state loads batched ahead of the updates; S_t is written in the blocked
+// layout the next delivery reads.
+struct LifFinish {
+    static constexpr bool kActive = true;
+    LifParams P;
+    float *v;
+    int *last;
+    __nv_bfloat16 *s_out;
+    int *counts;
+    int t;
+    __device__ void load(int idx, float &vv, int &ls) const {
+        vv = v[idx];
+        ls = last[idx];
+    }
+    __device__ bool update(int b, int j, int idx, float a, float vv, int ls) const {
+        const bool spk = lif_apply(P, a, vv, ls, t, idx);
+        v[idx] = vv;
+        last[idx] = ls;
+        s_out[s_blocked(b, j)] = __float2bfloat16_rn(spk ? 1.0f : 0.0f);
+        return spk;
+    }
+    __device__ void count(int k) const {
+        if (k) atomicAdd(counts, k);
+    }
+};
+
 } // namespace
 
 struct nbg_dense {
@@ -296,6 +332,7 @@ struct nbg_dense {
     DevBuf<__nv_bfloat16> whi, wlo, s[2];
     DevBuf<unsigned> bits[2];
     DevBuf<int> last, err;
+    DevBuf<unsigned int> tile_cnt; // fused-update arrivals per tile (zero between launches)
     std::vector<cudaEvent_t> dev_pool; // delivery start/stop events, 2 per step
     int next_t = 0;
     bool ran = false;
@@ -318,6 +355,7 @@ nbg_status dense_reset(nbg_dense *d) {
         NBG_CUDA(d->s[k].zero());
         NBG_CUDA(d->bits[k].zero());
     }
+    if (d->tile_cnt.p) NBG_CUDA(d->tile_cnt.zero());
     d->next_t = 0;
     d->ran = false;
     d->counts_host.clear();
@@ -328,8 +366,8 @@ nbg_status dense_reset(nbg_dense *d) {
 nbg_status launch_delivery(nbg_dense *d, int par) {
     if (d->precision == NBG_DENSE_SPLIT_BF16) {
         dim3 grid(d->N / umma::kM, kSplitK);
-        umma::k_dense_umma<<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
-            d->whi.p, d->wlo.p, d->s[par].p, d->partial.p, d->N, kSplitK, d->err.p);
+        umma::k_dense_umma<umma::NoFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
+            d->whi.p, d->wlo.p, d->s[par].p, d->partial.p, d->N, kSplitK, d->err.p, d->tile_cnt.p, umma::NoFinish{});
     } else if (d->precision == NBG_DENSE_SPLIT_BF16_SYNC) {
         dim3 grid(d->N / kBM, kSplitK);
         k_dense_gemm<<<grid, kGemmThreads, kGemmSmem, d->stream>>>(d->whi.p, d->wlo.p, d->s[par].p, d->partial.p,
@@ -415,8 +453,13 @@ nbg_status nbg_dense_create(int instances, int neurons, const float *w, const nb
             chk(cudaGetLastError());
             chk(cudaDeviceSynchronize());
             if (ce == cudaSuccess)
-                chk(cudaFuncSetAttribute(umma::k_dense_umma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                chk(cudaFuncSetAttribute(umma::k_dense_umma<umma::NoFinish>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, umma::kSmemBytes));
+            if (ce == cudaSuccess)
+                chk(cudaFuncSetAttribute(umma::k_dense_umma<LifFinish>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          umma::kSmemBytes));
+            if (ce == cudaSuccess) chk(d->tile_cnt.alloc((size_t)neurons / umma::kM));
+            if (ce == cudaSuccess) chk(d->tile_cnt.zero());
         } else if (ce == cudaSuccess) {
             dim3 grid(neurons / 32, neurons / 32), block(32, 8);
             k_split_transpose<<<grid, block>>>(tmp.p, d->whi.p, d->wlo.p, neurons);
@@ -481,6 +524,14 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
             const int t = d->next_t + k;
             const int in = (t + 1) & 1, outp = t & 1; // S_{t-1} lives in buffer (t-1)&1
             NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0)], d->stream));
+            if (blocked) { // tcgen05: delivery and update in one launch
+                const LifFinish fin{d->P, d->v.p, d->last.p, d->s[outp].p, dcnt.p + k, t};
+                dim3 grid(d->N / umma::kM, kSplitK);
+                umma::k_dense_umma<LifFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
+                    d->whi.p, d->wlo.p, d->s[in].p, d->partial.p, d->N, kSplitK, d->err.p, d->tile_cnt.p, fin);
+                NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0) + 1], d->stream));
+                continue;
+            }
             launch_delivery(d, in);
             NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0) + 1], d->stream));
             k_dense_lif<<<(total + 255) / 256, 256, 0, d->stream>>>(
@@ -578,8 +629,8 @@ nbg_status nbg_dense_deliver(nbg_dense *d, const uint8_t *s, float *out) {
             h[s_blocked((int)(i / d->N), (int)(i % d->N))] = __float2bfloat16_rn(s[i] ? 1.0f : 0.0f);
         NBG_CUDA(sb.upload(h));
         dim3 grid(d->N / umma::kM, kSplitK);
-        umma::k_dense_umma<<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(d->whi.p, d->wlo.p, sb.p, part.p,
-                                                                               d->N, kSplitK, d->err.p);
+        umma::k_dense_umma<umma::NoFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
+            d->whi.p, d->wlo.p, sb.p, part.p, d->N, kSplitK, d->err.p, d->tile_cnt.p, umma::NoFinish{});
     } else if (d->precision == NBG_DENSE_SPLIT_BF16_SYNC) {
         std::vector<__nv_bfloat16> h(tot);
         for (size_t i = 0; i < tot; ++i) h[i] = __float2bfloat16_rn(s[i] ? 1.0f : 0.0f);

@@ -144,29 +144,38 @@ __device__ __forceinline__ float hash_uniform01(int neuron_index, int time_step)
 // inputs: the rate is bias + gain * I_ext, identical to update_neuron below).
 __device__ __forceinline__ bool generator_fired(const NetDev &n, int k, int ts);
 
-__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
-    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
-    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
-    return z ^ (z >> 31);
+// Noise current: Irwin-Hall sum of twelve 16-bit uniforms (u + 1/2) / 2^16
+// minus 6, summed in integers and converted once (exact in float).  Bits
+// from the PCG RXS-M-XS 32-bit output permutation used as a hash (Jarzynski
+// and Olano, "Hash Functions for GPU Rendering", JCGT 2020): a per-neuron key
+// from (seed, neuron), a per-step key from (neuron key, step), then six
+// 32-bit words of two uniforms each.  Identical arithmetic in the oracle.
+__device__ __forceinline__ unsigned int pcg_hash(unsigned int v) {
+    const unsigned int state = v * 747796405u + 2891336453u;
+    const unsigned int word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
 }
-
-// Irwin-Hall(12) approximation of N(0,1), integer sum converted once.
-__device__ __forceinline__ float gauss12(unsigned long long seed, int neuron, int t) {
+__device__ __forceinline__ unsigned int noise_key(unsigned long long seed, int neuron) {
+    return pcg_hash((unsigned int)neuron ^ pcg_hash((unsigned int)seed ^ (unsigned int)(seed >> 32)));
+}
+__device__ __forceinline__ float gauss12(unsigned int key, int t) {
+    const unsigned int tk = pcg_hash(key ^ ((unsigned int)t * 0x9E3779B9u));
     int m = 0;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        unsigned long long h = mix64(seed + (unsigned long long)(unsigned int)neuron * 0x9E3779B97F4A7C15ULL +
-                                     ((unsigned long long)(unsigned int)t * 6ull + (unsigned long long)k) *
-                                         0xD1B54A32D192ED03ULL);
-        m += (int)(h & 0xFFFFFFu) + (int)((h >> 32) & 0xFFFFFFu);
+    for (unsigned int k = 0; k < 6; ++k) {
+        const unsigned int h = pcg_hash(tk + k);
+        m += (int)(h & 0xFFFFu) + (int)(h >> 16);
     }
-    return (float)(m - 6 * 16777216) * (1.0f / 16777216.0f);
+    return (float)(m + 6 - 6 * 65536) * (1.0f / 65536.0f);
 }
 
+// Current-based Izhikevich right-hand side with explicit fused multiply-adds
+// (each rounded once; the oracle writes the same fmaf calls):
+//   f = (fma(fma(0.04, v, 5), v, 140) - u) + I,   g = a * fma(b, v, -u)
 __device__ __forceinline__ float izh_f(float v, float u, float I) {
-    return 0.04f * v * v + 5.0f * v + 140.0f - u + I;
+    return (__fmaf_rn(__fmaf_rn(0.04f, v, 5.0f), v, 140.0f) - u) + I;
 }
-__device__ __forceinline__ float izh_g(float a, float b, float v, float u) { return a * (b * v - u); }
+__device__ __forceinline__ float izh_g(float a, float b, float v, float u) { return a * __fmaf_rn(b, v, -u); }
 
 struct NeuronRegs {
     float v, u, gexc, ginh, iext;
@@ -386,7 +395,7 @@ __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, i
 }
 
 // One neuron update; returns true on a spike.  `noise` is
-// sigma * gauss12(seed, j, t) for noisy IZH_RK4 layers (else 0).
+// sigma * gauss12(noise_key(seed, j), t) for noisy IZH_RK4 layers (else 0).
 __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, NeuronRegs &r, float acc_a,
                                              float acc_b, float noise, int j, int t) {
     switch (M.model) {
@@ -470,14 +479,14 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
             const float h = n.dt, hh = 0.5f * n.dt, h6 = n.dt / 6.0f;
             const float v = r.v, u = r.u;
             const float k1v = izh_f(v, u, I), k1u = izh_g(a, b, v, u);
-            const float v2 = v + hh * k1v, u2 = u + hh * k1u;
+            const float v2 = __fmaf_rn(hh, k1v, v), u2 = __fmaf_rn(hh, k1u, u);
             const float k2v = izh_f(v2, u2, I), k2u = izh_g(a, b, v2, u2);
-            const float v3 = v + hh * k2v, u3 = u + hh * k2u;
+            const float v3 = __fmaf_rn(hh, k2v, v), u3 = __fmaf_rn(hh, k2u, u);
             const float k3v = izh_f(v3, u3, I), k3u = izh_g(a, b, v3, u3);
-            const float v4 = v + h * k3v, u4 = u + h * k3u;
+            const float v4 = __fmaf_rn(h, k3v, v), u4 = __fmaf_rn(h, k3u, u);
             const float k4v = izh_f(v4, u4, I), k4u = izh_g(a, b, v4, u4);
-            r.v = v + h6 * (k1v + 2.0f * k2v + 2.0f * k3v + k4v);
-            r.u = u + h6 * (k1u + 2.0f * k2u + 2.0f * k3u + k4u);
+            r.v = __fmaf_rn(h6, __fmaf_rn(2.0f, k3v, __fmaf_rn(2.0f, k2v, k1v)) + k4v, v);
+            r.u = __fmaf_rn(h6, __fmaf_rn(2.0f, k3u, __fmaf_rn(2.0f, k2u, k1u)) + k4u, u);
         }
         r.last += 1;
         if (r.v >= M.p[4]) {
@@ -640,11 +649,9 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
             gin[q].pos = n.gen_pos[g0 + q];
         }
     }
-    float nz[kMaxBlockSteps];
-    if (active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f) {
-#pragma unroll 4
-        for (int b = 0; b < B; ++b) nz[b] = L.p[5] * gauss12(n.seed, j, T0 + b);
-    }
+    // noisy RK4 neurons: per-neuron noise key (the per-step draw is made in the step loop)
+    const bool noisy = active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f;
+    const unsigned int nkey = noisy ? noise_key(n.seed, j) : 0u;
     // Fast path (in-degree <= 1024, <= 32 generator inputs): the L2-resident
     // word summary says which of this neuron's mask words hold arrivals, so
     // only those words are loaded from HBM.  Two-stage prefetch: the summary
@@ -693,7 +700,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
 #pragma unroll
                 for (int q = 0; q < kGenCached; ++q) {
                     const int ts = t - gin[q].delay;
-                    if (ts >= 0 && hash_uniform01(gin[q].local, ts) < gin[q].prob) {
+                    if (g0 + q < g1 && ts >= 0 && hash_uniform01(gin[q].local, ts) < gin[q].prob) {
                         gfired |= 1u << q;
                         gwords |= 1u << (gin[q].pos >> 5);
                     }
@@ -743,7 +750,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
                 // this neuron's summary bits (set while its words were non-zero)
                 summary_clear_range(n.wsum + (size_t)slot * n.Ws, woff, nw);
             }
-            spk = update_neuron(n, L, r, acc_a, acc_b, nz[b], j, t);
+            spk = update_neuron(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
         }
         if (spk) spk_steps |= 1u << b;

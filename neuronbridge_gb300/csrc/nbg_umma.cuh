@@ -25,6 +25,15 @@
 // Every wait on an mbarrier is bounded (clock64 deadline); on expiry the CTA
 // records kUmmaTimeout in the error word, stops issuing, waits (bounded) for
 // the MMAs it already issued, frees its TMEM and returns.
+//
+// Fused step (split = 2): with an active `Finish` functor, the CTA that
+// completes a tile (the second of its two split-K contributors to arrive,
+// found with one atomic per CTA on a per-tile counter after every thread's
+// release fence; nothing waits) adds the other CTA's partial to the
+// accumulator it still holds in registers (two-term float addition is
+// commutative, so the sum equals partial 0 + partial 1 whichever CTA
+// finishes) and runs the functor on each of its elements -- the neuron
+// update of the step -- then rearms the counter for the next launch.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -141,10 +150,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 // partial[ks][b][j] for the CTA's 128 post neurons and K range (split ks).
 // wt_hi / wt_lo: blocked W^T, block (m tile, k chunk) at ((mt * kchunks + kc) * kBlockA);
 // s_blk: blocked S, block kc at kc * kBlockB.
+// No fused update: the partial sums are the result.
+struct NoFinish {
+    static constexpr bool kActive = false;
+    __device__ void load(int, float &, int &) const {}
+    __device__ bool update(int, int, int, float, float, int) const { return false; }
+    __device__ void count(int) const {}
+};
+
+template <class Finish>
 __global__ void __launch_bounds__(kThreads, 1)
     k_dense_umma(const __nv_bfloat16 *__restrict__ wt_hi, const __nv_bfloat16 *__restrict__ wt_lo,
                  const __nv_bfloat16 *__restrict__ s_blk, float *__restrict__ partial, int n, int split,
-                 int *__restrict__ err) {
+                 int *__restrict__ err, unsigned int *__restrict__ tile_cnt, const Finish fin) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(stages + kUStages * kStageBytes);
@@ -219,24 +237,53 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_wait(done, 0, abort);
     __syncthreads();
     fence_after();
+    const int q = warp & 3, h = warp >> 2;
+    const int j = mt * kM + 32 * q + lane;
+    float acc[2][16];
     if (!*abort) {
-        const int q = warp & 3, h = warp >> 2;
-        const int j = mt * kM + 32 * q + lane;
         float *out = partial + (size_t)ks * kN * n;
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * h), acc[0]);
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * h + 16), acc[1]);
 #pragma unroll
-        for (int part = 0; part < 2; ++part) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * h + 16 * part), v);
-#pragma unroll
-            for (int c = 0; c < 16; ++c) out[(size_t)(32 * h + 16 * part + c) * n + j] = v[c];
-        }
+        for (int c = 0; c < 32; ++c) out[(size_t)(32 * h + c) * n + j] = acc[c >> 4][c & 15];
     }
     fence_before();
+    if constexpr (Finish::kActive) __threadfence(); // this thread's partial before the CTA's arrival
     __syncthreads();
     if (threadIdx.x == 0 && *abort) atomicOr(err, kUmmaTimeout);
     if (warp == 2) {
         fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+    if constexpr (Finish::kActive) {
+        __shared__ int finisher;
+        if (threadIdx.x == 0)
+            finisher = !*abort && atomicAdd(&tile_cnt[mt], 1u) == (unsigned int)(split - 1);
+        __syncthreads();
+        if (finisher) {
+            __threadfence(); // the other contributor's partial is visible after its arrival
+            const float *other = partial + (size_t)(ks ^ 1) * kN * n;
+            int spikes = 0;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) { // loads of 16 elements in flight, then their updates
+                float oth[16], vv[16];
+                int ls[16];
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const int idx = (32 * h + 16 * half + c) * n + j;
+                    oth[c] = __ldcg(other + idx);
+                    fin.load(idx, vv[c], ls[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    const int b = 32 * h + 16 * half + c;
+                    spikes += fin.update(b, j, b * n + j, acc[half][c] + oth[c], vv[c], ls[c]) ? 1 : 0;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) spikes += __shfl_down_sync(0xffffffffu, spikes, o);
+            if (lane == 0) fin.count(spikes);
+            if (threadIdx.x == 0) tile_cnt[mt] = 0u;
+        }
     }
 }
 

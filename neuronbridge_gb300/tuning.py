@@ -13,7 +13,9 @@ from .simulation import Simulation
 
 def candidates(block_limit: int) -> list[tuple[int, int]]:
     steps = sorted({block_limit, max(1, block_limit // 2), max(1, (2 * block_limit) // 3)}, reverse=True)
-    return [(t, b) for t in (128, 256, 64) for b in steps]
+    # 32-thread blocks let the block scheduler spread a small network's warps
+    # evenly over the SMs (one wave, no SM holding a whole extra block)
+    return [(t, b) for t in (128, 256, 64, 32) for b in steps]
 
 
 def autotune(sim: Simulation, trial_steps: int = 300, repeats: int = 2) -> dict:

@@ -167,22 +167,29 @@ static float hash_uniform01(int neuron_index, int time_step) {
 }
 
 /* Counter-based N(0,1) approximation for the Izhikevich noise current: the
- * Irwin-Hall sum of twelve 24-bit uniforms minus 6, summed in integers and
- * converted once.  Bits come from the splitmix64 finaliser keyed by
- * (seed, neuron, step).  Not part of the reference (it has no seeded noise). */
-static uint64_t mix64(uint64_t z) {
-    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
-    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
-    return z ^ (z >> 31);
+ * Irwin-Hall sum of twelve 16-bit uniforms (u + 1/2) / 2^16 minus 6, summed in
+ * integers and converted once (exact in float).  Bits come from the PCG
+ * RXS-M-XS 32-bit output permutation used as a hash (Jarzynski and Olano,
+ * "Hash Functions for GPU Rendering", JCGT 9(3), 2020): a per-neuron key
+ * from (seed, neuron), a per-step key from (neuron key, step), then six
+ * 32-bit words (two uniforms each).  Not part of the reference (it has no
+ * seeded noise). */
+static uint32_t pcg_hash(uint32_t v) {
+    uint32_t state = v * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+static uint32_t noise_key(uint64_t seed, int neuron) {
+    return pcg_hash((uint32_t)neuron ^ pcg_hash((uint32_t)seed ^ (uint32_t)(seed >> 32)));
 }
 static REAL gauss12(uint64_t seed, int neuron, int t) {
+    uint32_t tk = pcg_hash(noise_key(seed, neuron) ^ ((uint32_t)t * 0x9E3779B9u));
     int32_t m = 0;
-    for (int k = 0; k < 6; ++k) {
-        uint64_t h = mix64(seed + (uint64_t)(uint32_t)neuron * 0x9E3779B97F4A7C15ULL +
-                           ((uint64_t)(uint32_t)t * 6u + (uint64_t)k) * 0xD1B54A32D192ED03ULL);
-        m += (int32_t)(h & 0xFFFFFFu) + (int32_t)((h >> 32) & 0xFFFFFFu);
+    for (uint32_t k = 0; k < 6; ++k) {
+        uint32_t h = pcg_hash(tk + k);
+        m += (int32_t)(h & 0xFFFFu) + (int32_t)(h >> 16);
     }
-    return (REAL)(m - 6 * 16777216) * (REAL)(1.0 / 16777216.0);
+    return (REAL)(m + 6 - 6 * 65536) * (REAL)(1.0 / 65536.0);
 }
 
 static void set_err(char *err, int errlen, const char *msg) {
@@ -624,8 +631,17 @@ static int spiked_izh_cond(net_t *n, layer_t *L, int i) {
  * plus Gaussian noise held constant over the step.  The reference registers
  * only forward Euler (L/ModelFactory/IntegrationMethodList.inc:9-12); this
  * model follows its Izhikevich equations, reset and LastSpike gating. */
-static REAL izh_f(REAL v, REAL u, REAL I) { return K(0.04) * v * v + K(5.0) * v + K(140.0) - u + I; }
-static REAL izh_g(REAL a, REAL b, REAL v, REAL u) { return a * (b * v - u); }
+/* Current-based Izhikevich right-hand side (config 1; the reference has only
+ * the conductance/Euler form).  Written with explicit fused multiply-adds,
+ * each rounded once, identically in the CUDA kernel:
+ *   f = (fma(fma(0.04, v, 5), v, 140) - u) + I,   g = a * fma(b, v, -u). */
+#ifdef REAL_IS_DOUBLE
+#define FMA(x, y, z) fma((x), (y), (z))
+#else
+#define FMA(x, y, z) fmaf((x), (y), (z))
+#endif
+static REAL izh_f(REAL v, REAL u, REAL I) { return (FMA(FMA(K(0.04), v, K(5.0)), v, K(140.0)) - u) + I; }
+static REAL izh_g(REAL a, REAL b, REAL v, REAL u) { return a * FMA(b, v, -u); }
 static int spiked_izh_rk4(net_t *n, layer_t *L, int i, int t) {
     REAL a = L->f[0], b = L->f[1];
     REAL I = n->g_ampa[i] + n->i_ext[i];
@@ -634,15 +650,16 @@ static int spiked_izh_rk4(net_t *n, layer_t *L, int i, int t) {
     if (n->last[i] > 0) {
         REAL h = n->dt, hh = K(0.5) * n->dt, h6 = n->dt / K(6.0);
         REAL v = n->v[i], u = n->u[i];
+        /* classical RK4; stage combinations as fused multiply-adds */
         REAL k1v = izh_f(v, u, I), k1u = izh_g(a, b, v, u);
-        REAL v2 = v + hh * k1v, u2 = u + hh * k1u;
+        REAL v2 = FMA(hh, k1v, v), u2 = FMA(hh, k1u, u);
         REAL k2v = izh_f(v2, u2, I), k2u = izh_g(a, b, v2, u2);
-        REAL v3 = v + hh * k2v, u3 = u + hh * k2u;
+        REAL v3 = FMA(hh, k2v, v), u3 = FMA(hh, k2u, u);
         REAL k3v = izh_f(v3, u3, I), k3u = izh_g(a, b, v3, u3);
-        REAL v4 = v + h * k3v, u4 = u + h * k3u;
+        REAL v4 = FMA(h, k3v, v), u4 = FMA(h, k3u, u);
         REAL k4v = izh_f(v4, u4, I), k4u = izh_g(a, b, v4, u4);
-        n->v[i] = v + h6 * (k1v + K(2.0) * k2v + K(2.0) * k3v + k4v);
-        n->u[i] = u + h6 * (k1u + K(2.0) * k2u + K(2.0) * k3u + k4u);
+        n->v[i] = FMA(h6, FMA(K(2.0), k3v, FMA(K(2.0), k2v, k1v)) + k4v, v);
+        n->u[i] = FMA(h6, FMA(K(2.0), k3u, FMA(K(2.0), k2u, k1u)) + k4u, u);
     }
     n->last[i] += 1;
     if (n->v[i] >= L->f[5]) {

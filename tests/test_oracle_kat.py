@@ -99,4 +99,11 @@ def test_fp64_oracle_tracks_fp32_on_short_horizon(oracle_lib):
     a.run(50)
     b.run(50)
     va, vb = a.state(0), b.state(0)
-    assert np.max(np.abs(va - vb)) < 1e-3
+    ta, ia = a.spikes()
+    tb, ib = b.spikes()
+    assert np.array_equal(ta, tb) and np.array_equal(ia, ib)
+    # FP32 rounding stays small below the upswing; a neuron mid-upswing
+    # (v > -40 mV, where dv/dv grows like 0.08 v + 5) amplifies it
+    sub = vb < -40.0
+    assert np.max(np.abs(va - vb)[sub]) < 1e-3
+    assert np.median(np.abs(va - vb)) < 1e-4
