@@ -367,7 +367,8 @@ nbg_status launch_delivery(nbg_dense *d, int par) {
     if (d->precision == NBG_DENSE_SPLIT_BF16) {
         dim3 grid(d->N / umma::kM, kSplitK);
         umma::k_dense_umma<umma::NoFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
-            d->whi.p, d->wlo.p, d->s[par].p, d->partial.p, d->N, kSplitK, d->err.p, d->tile_cnt.p, umma::NoFinish{});
+            d->whi.p, d->wlo.p, d->s[par].p, d->partial.p, d->N, kSplitK, 0, d->err.p, d->tile_cnt.p,
+            umma::NoFinish{});
     } else if (d->precision == NBG_DENSE_SPLIT_BF16_SYNC) {
         dim3 grid(d->N / kBM, kSplitK);
         k_dense_gemm<<<grid, kGemmThreads, kGemmSmem, d->stream>>>(d->whi.p, d->wlo.p, d->s[par].p, d->partial.p,
@@ -528,7 +529,8 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
                 const LifFinish fin{d->P, d->v.p, d->last.p, d->s[outp].p, dcnt.p + k, t};
                 dim3 grid(d->N / umma::kM, kSplitK);
                 umma::k_dense_umma<LifFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
-                    d->whi.p, d->wlo.p, d->s[in].p, d->partial.p, d->N, kSplitK, d->err.p, d->tile_cnt.p, fin);
+                    d->whi.p, d->wlo.p, d->s[in].p, d->partial.p, d->N, kSplitK, t & 1, d->err.p, d->tile_cnt.p,
+                    fin);
                 NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0) + 1], d->stream));
                 continue;
             }
@@ -630,7 +632,7 @@ nbg_status nbg_dense_deliver(nbg_dense *d, const uint8_t *s, float *out) {
         NBG_CUDA(sb.upload(h));
         dim3 grid(d->N / umma::kM, kSplitK);
         umma::k_dense_umma<umma::NoFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
-            d->whi.p, d->wlo.p, sb.p, part.p, d->N, kSplitK, d->err.p, d->tile_cnt.p, umma::NoFinish{});
+            d->whi.p, d->wlo.p, sb.p, part.p, d->N, kSplitK, 0, d->err.p, d->tile_cnt.p, umma::NoFinish{});
     } else if (d->precision == NBG_DENSE_SPLIT_BF16_SYNC) {
         std::vector<__nv_bfloat16> h(tot);
         for (size_t i = 0; i < tot; ++i) h[i] = __float2bfloat16_rn(s[i] ? 1.0f : 0.0f);

@@ -162,7 +162,7 @@ template <class Finish>
 __global__ void __launch_bounds__(kThreads, 1)
     k_dense_umma(const __nv_bfloat16 *__restrict__ wt_hi, const __nv_bfloat16 *__restrict__ wt_lo,
                  const __nv_bfloat16 *__restrict__ s_blk, float *__restrict__ partial, int n, int split,
-                 int *__restrict__ err, unsigned int *__restrict__ tile_cnt, const Finish fin) {
+                 int reverse, int *__restrict__ err, unsigned int *__restrict__ tile_cnt, const Finish fin) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(stages + kUStages * kStageBytes);
@@ -203,11 +203,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int s = it % kUStages;
             if (it >= kUStages && !mbar_wait(&empty[s], ((it / kUStages) & 1) ^ 1, abort)) break;
             uint8_t *st = stages + s * kStageBytes;
-            const size_t blk = (size_t)mt * kchunks + kc0 + it;
+            // K chunks in ascending order, or descending when `reverse`: the
+            // chunks a step streams last are still in L2 when the next step,
+            // run in the other direction, streams them first
+            const int kc = reverse ? kc0 + iters - 1 - it : kc0 + it;
+            const size_t blk = (size_t)mt * kchunks + kc;
             mbar_expect_tx(&full[s], kStageBytes);
             bulk_copy(st, (const uint8_t *)wt_hi + blk * kBlockA, kBlockA, &full[s]);
             bulk_copy(st + kBlockA, (const uint8_t *)wt_lo + blk * kBlockA, kBlockA, &full[s]);
-            bulk_copy(st + 2 * kBlockA, (const uint8_t *)s_blk + (size_t)(kc0 + it) * kBlockB, kBlockB, &full[s]);
+            bulk_copy(st + 2 * kBlockA, (const uint8_t *)s_blk + (size_t)kc * kBlockB, kBlockB, &full[s]);
         }
     } else if (warp == 1 && lane == 0) { // MMA issuer
         constexpr uint32_t idesc = make_idesc();

@@ -179,7 +179,8 @@ def test_launch_shape_invariance():
     net, cfg = workloads.izhikevich_stdp(n=4000, in_degree=50)
     ref = nb.Simulation(net, cfg, seed=2)
     ref.run(1500)
-    for kw in ({"block_steps": 1}, {"block_steps": 3, "threads_per_block": 64}, {"use_graph": False}):
+    for kw in ({"block_steps": 1}, {"block_steps": 3, "threads_per_block": 64}, {"threads_per_block": 32},
+               {"use_graph": False}):
         s = nb.Simulation(net, cfg, seed=2, **kw)
         s.run(1500)
         assert _raster_equal(ref.spike_raster(), s.spike_raster()), kw
