@@ -182,6 +182,15 @@ nbg_status nbg_set_state(nbg_engine *e, int field, const float *in /* n_neurons 
 nbg_status nbg_num_spikes(nbg_engine *e, int64_t *n);
 nbg_status nbg_get_spikes(nbg_engine *e, int32_t *times, int32_t *ids, int64_t capacity);
 nbg_status nbg_clear_spikes(nbg_engine *e);
+/* Entries [offset, offset + count) of the recorded spikes (a monitor reading
+ * only what the last run call added). */
+nbg_status nbg_get_spikes_from(nbg_engine *e, int64_t offset, int64_t count, int32_t *times, int32_t *ids);
+/* Record (or stop recording) the spikes of layer `layer` in the raster.  At
+ * create a layer is recorded iff it is an output; the DebugMonitor also
+ * records the layers of the neurons it watches (the reference's
+ * Simulation::WriteSpike feeds the monitor for every spike,
+ * Simulation.cu:611-633).  Takes effect from the next run call. */
+nbg_status nbg_set_layer_record(nbg_engine *e, int layer, int record);
 /* delivered synaptic events accumulated over all run calls */
 nbg_status nbg_num_events(nbg_engine *e, int64_t *n);
 

@@ -10,9 +10,13 @@ from ._lib import NbgError, load
 from .model import (CATALOG, Connection, LearningRule, NativeParameter, Network, NetworkDescription, NeuronLayer,
                     SimulationConfig, float32, float32_list, float64, int32, resolve_model)
 from .simulation import Simulation
+from . import nbnet
+from .debug_monitor import DebugMonitorConfig, DebugMonitorResult, open_debug_monitor
+from .nbnet import StreamingBuildOptions
 
 __all__ = [
     "CATALOG", "Connection", "LearningRule", "NativeParameter", "NbgError", "Network", "NetworkDescription",
     "NeuronLayer", "Simulation", "SimulationConfig", "float32", "float32_list", "float64", "int32", "load",
-    "resolve_model",
+    "resolve_model", "nbnet", "StreamingBuildOptions", "DebugMonitorConfig", "DebugMonitorResult",
+    "open_debug_monitor",
 ]

@@ -97,6 +97,8 @@ _SIGNATURES = {
     "nbg_get_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p, _f32p, _f32p, _i32p]),
     "nbg_set_weight": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_float]),
     "nbg_set_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p]),
+    "nbg_get_spikes_from": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, _i32p, _i32p]),
+    "nbg_set_layer_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "nbg_add_external_spikes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _i32p, _i32p]),
     "nbg_add_external_currents": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _i32p, _i32p, _f32p]),
     "nbg_set_current_at": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float]),

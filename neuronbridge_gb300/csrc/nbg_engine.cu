@@ -1792,6 +1792,28 @@ nbg_status nbg_get_spikes(nbg_engine *e, int32_t *times, int32_t *ids, int64_t c
     return NBG_OK;
 }
 
+nbg_status nbg_get_spikes_from(nbg_engine *e, int64_t offset, int64_t count, int32_t *times, int32_t *ids) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    const int64_t n = (int64_t)e->spk_id.size();
+    if (offset < 0 || count < 0 || offset + count > n)
+        return fail(NBG_ERR_INVALID, "spike range [%lld, %lld) outside the %lld recorded spikes", (long long)offset,
+                    (long long)(offset + count), (long long)n);
+    if (count && times) std::memcpy(times, e->spk_t.data() + offset, count * sizeof(int32_t));
+    if (count && ids) std::memcpy(ids, e->spk_id.data() + offset, count * sizeof(int32_t));
+    return NBG_OK;
+}
+
+nbg_status nbg_set_layer_record(nbg_engine *e, int layer, int record) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (layer < 0 || layer >= (int)e->layers.size()) return fail(NBG_ERR_INVALID, "layer %d out of range", layer);
+    if ((e->layers[layer].record != 0) == (record != 0)) return NBG_OK;
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    e->layers[layer].record = record != 0 ? 1 : 0;
+    NBG_CUDA(cudaMemcpy(e->d_layers.p + layer, &e->layers[layer], sizeof(LayerDev), cudaMemcpyHostToDevice));
+    return NBG_OK;
+}
+
 nbg_status nbg_clear_spikes(nbg_engine *e) {
     if (!e) return fail(NBG_ERR_INVALID, "null engine");
     e->spk_t.clear();

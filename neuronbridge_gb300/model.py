@@ -323,6 +323,7 @@ class NetworkDescription:
         self.layer_fparams = np.zeros((n, _lib.NFP), np.float32)
         self.layer_iparams = np.zeros((n, _lib.NIP), np.int32)
         self.layer_output = np.zeros(n, bool)
+        self.layer_monitored = np.zeros(n, bool)
         for i, layer in enumerate(layers):
             mid, f, ip = layer.native_params()
             self.layer_model[i] = mid
@@ -330,6 +331,7 @@ class NetworkDescription:
             self.layer_fparams[i] = f
             self.layer_iparams[i] = ip
             self.layer_output[i] = layer.output
+            self.layer_monitored[i] = layer.monitored
         parts = [c.normalized() for c in connections]
         cat = lambda key, dt: (np.concatenate([p[key] for p in parts]).astype(dt, copy=False)
                                if parts else np.zeros(0, dt))

@@ -12,6 +12,9 @@ otherwise.
 from __future__ import annotations
 
 import ctypes
+import os
+import time
+from pathlib import Path
 
 import numpy as np
 
@@ -66,19 +69,34 @@ def make_desc(flat: dict):
 class Simulation:
     """High-level facade over one GB300 engine instance."""
 
-    def __init__(self, network: Network | NetworkDescription, config: SimulationConfig, *, device: int = 0,
-                 semantics: str = "legacy_cpu", seed: int = 0, block_steps: int = 0, use_graph: bool = True,
-                 threads_per_block: int = 256, spike_capacity: int = 0, event_log_capacity: int = 0,
-                 kernel_timing: bool = False):
+    def __init__(self, network: Network | NetworkDescription | str | os.PathLike, config: SimulationConfig, *,
+                 build_options=None, device: int = 0, semantics: str = "legacy_cpu", seed: int = 0,
+                 block_steps: int = 0, use_graph: bool = True, threads_per_block: int = 256,
+                 spike_capacity: int = 0, event_log_capacity: int = 0, kernel_timing: bool = False):
         if not isinstance(config, SimulationConfig):
             raise TypeError("Simulation expects a neuronbridge_gb300.SimulationConfig")
         if semantics not in _SEMANTICS:
             raise ValueError(f"semantics must be one of {sorted(_SEMANTICS)}")
+        build_started = time.perf_counter()
         self.config = config
         self.lib = _lib.load()
-        native = network.to_native() if isinstance(network, Network) else network
-        if not isinstance(native, NetworkDescription):
-            raise TypeError("Simulation expects a neuronbridge_gb300.Network")
+        if isinstance(network, (str, os.PathLike)):  # .nbnet file (the reference's path overload)
+            from . import nbnet
+
+            options = build_options or nbnet.StreamingBuildOptions()
+            if not isinstance(options, nbnet.StreamingBuildOptions):
+                raise TypeError("build_options must be a StreamingBuildOptions")
+            native, self._build_stats = nbnet.load(network, options)
+            self.network_file = Path(network).resolve()
+        else:
+            if build_options is not None:
+                raise TypeError("build_options is only valid when Simulation receives an .nbnet path")
+            native = network.to_native() if isinstance(network, Network) else network
+            if not isinstance(native, NetworkDescription):
+                raise TypeError("Simulation expects a neuronbridge_gb300.Network or an .nbnet path")
+            self.network_file = None
+            self._build_stats = {"mode": "in_memory", "neuron_count": native.neuron_count,
+                                 "connection_count": int(len(native.source))}
         self.description = native
         self.flat = native.flat(config.timestep, _SEMANTICS[semantics], seed)
         desc, keep = make_desc(self.flat)
@@ -105,6 +123,15 @@ class Simulation:
             if out:
                 self._output_mask[layer_start[i]:layer_start[i + 1]] = True
         self._layer_of = np.repeat(np.arange(len(native.layer_count)), native.layer_count)
+        self._layer_monitored = native.layer_monitored
+        self._extra_recorded = False  # layers recorded for the monitor beyond the outputs
+        self._monitor = None
+        self._build_stats["total_build_seconds"] = time.perf_counter() - build_started
+
+    @property
+    def build_stats(self) -> dict:
+        """Construction-path diagnostics (the reference's Simulation.build_stats)."""
+        return dict(self._build_stats)
 
     # -------------------------------------------------------------- lifecycle
     def close(self) -> None:
@@ -133,12 +160,64 @@ class Simulation:
             raise ValueError("Simulation.run steps must be positive")
         self.init()
         _lib.check(self.lib.nbg_run(self._h, steps))
+        if self._monitor is not None:
+            self._monitor.capture(self.next_time - 1)
         return self
 
     def reset(self) -> "Simulation":
+        if self._monitor is not None:
+            self._monitor.collect_spikes()
         _lib.check(self.lib.nbg_reset(self._h))
+        if self._monitor is not None:
+            self._monitor.read = 0
         self._initialized = False
         return self
+
+    # --------------------------------------------------------- debug monitor
+    def enable_debug_monitor(self, config) -> "Simulation":
+        """Write CSV frames of state, spikes and weights at the end of every
+        run call (the reference's Simulation.enable_debug_monitor)."""
+        from .debug_monitor import DebugMonitor, DebugMonitorConfig
+
+        if not isinstance(config, DebugMonitorConfig):
+            raise TypeError("enable_debug_monitor expects a DebugMonitorConfig")
+        if self._monitor is not None:
+            self._monitor.close()
+            self._monitor = None
+        if config.enabled:
+            self._monitor = DebugMonitor(self, config)
+        self._debug_monitor_config = config
+        return self
+
+    def disable_debug_monitor(self) -> "Simulation":
+        if self._monitor is not None:
+            self._monitor.close()
+            self._monitor = None
+        return self
+
+    def flush_debug_monitor(self) -> "Simulation":
+        if self._monitor is not None:
+            self._monitor.flush()
+        return self
+
+    def result(self):
+        from .debug_monitor import DebugMonitorResult
+
+        if getattr(self, "_debug_monitor_config", None) is None:
+            raise RuntimeError("DebugMonitor is not enabled for this Simulation")
+        return DebugMonitorResult(self._debug_monitor_config.output_dir)
+
+    def _num_raster(self) -> int:
+        n = ctypes.c_int64()
+        _lib.check(self.lib.nbg_num_spikes(self._h, ctypes.byref(n)))
+        return n.value
+
+    def _raster_range(self, offset: int, count: int) -> tuple[np.ndarray, np.ndarray]:
+        t = np.empty(count, np.int32)
+        i = np.empty(count, np.int32)
+        _lib.check(self.lib.nbg_get_spikes_from(self._h, int(offset), int(count), _p(t, ctypes.c_int32),
+                                                _p(i, ctypes.c_int32)))
+        return t, i
 
     # ------------------------------------------------------------------ state
     @property
@@ -213,6 +292,9 @@ class Simulation:
         t = np.empty(n.value, np.int32)
         i = np.empty(n.value, np.int32)
         _lib.check(self.lib.nbg_get_spikes(self._h, _p(t, ctypes.c_int32), _p(i, ctypes.c_int32), n.value))
+        if self._extra_recorded:  # the monitor also records non-output layers
+            keep = self._output_mask[i]
+            t, i = t[keep], i[keep]
         return t, i
 
     def output_spikes(self) -> list[dict]:
@@ -221,7 +303,11 @@ class Simulation:
         return [{"time": int(a), "neuron_id": int(b)} for a, b in zip(t[keep], i[keep])]
 
     def clear_spikes(self) -> "Simulation":
+        if self._monitor is not None:
+            self._monitor.collect_spikes()
         _lib.check(self.lib.nbg_clear_spikes(self._h))
+        if self._monitor is not None:
+            self._monitor.read = 0
         return self
 
     @property

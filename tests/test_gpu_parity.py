@@ -260,3 +260,22 @@ def test_weight_snapshot_round_trip(tmp_path, oracle_lib):
     bad.write_text("NPGR_WEIGHT_SNAPSHOT 1\ntime_step 0\nblock main 0 1\nrle\n1 0.5\nend_block\nend\n")
     with pytest.raises(RuntimeError, match="LoadWeight failed: main weight block count does not match"):
         b.load_weights(bad)
+
+
+def test_nbnet_path_simulation_equals_in_memory(tmp_path, oracle_lib):
+    """Simulation(path) streams a .nbnet file (small memory budget, several
+    batches) into the same engine state as Simulation(network)."""
+    from neuronbridge_gb300 import nbnet
+
+    net, cfg = workloads.izhikevich_stdp(n=3000, in_degree=60)
+    path = tmp_path / "izh.nbnet"
+    nbnet.from_network(net, path)
+    a = nb.Simulation(net, cfg, seed=2)
+    b = nb.Simulation(path, cfg, seed=2, build_options=nbnet.StreamingBuildOptions(memory_budget_mb=1))
+    assert b.build_stats["runtime_build_path"] == "streaming_direct"
+    assert b.build_stats["connection_count"] == 180000
+    a.run(800)
+    b.run(800)
+    assert _raster_equal(a.spike_raster(), b.spike_raster())
+    assert np.array_equal(a.weights()["weight"], b.weights()["weight"])
+    assert np.array_equal(a.state_field(0), b.state_field(0))
