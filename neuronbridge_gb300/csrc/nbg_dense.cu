@@ -524,16 +524,24 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
         for (int k = k0; k < k1; ++k) {
             const int t = d->next_t + k;
             const int in = (t + 1) & 1, outp = t & 1; // S_{t-1} lives in buffer (t-1)&1
-            NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0)], d->stream));
-            if (blocked) { // tcgen05: delivery and update in one launch
+            if (blocked) { // tcgen05: delivery and update in one launch, back to back (PDL)
                 const LifFinish fin{d->P, d->v.p, d->last.p, d->s[outp].p, dcnt.p + k, t};
-                dim3 grid(d->N / umma::kM, kSplitK);
-                umma::k_dense_umma<LifFinish><<<grid, umma::kThreads, umma::kSmemBytes, d->stream>>>(
-                    d->whi.p, d->wlo.p, d->s[in].p, d->partial.p, d->N, kSplitK, t & 1, d->err.p, d->tile_cnt.p,
-                    fin);
-                NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0) + 1], d->stream));
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(d->N / umma::kM, kSplitK);
+                cfg.blockDim = dim3(umma::kThreads);
+                cfg.dynamicSmemBytes = umma::kSmemBytes;
+                cfg.stream = d->stream;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+                attr[0].val.programmaticStreamSerializationAllowed = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                NBG_CUDA(cudaLaunchKernelEx(&cfg, umma::k_dense_umma<LifFinish>, (const __nv_bfloat16 *)d->whi.p,
+                                            (const __nv_bfloat16 *)d->wlo.p, (const __nv_bfloat16 *)d->s[in].p,
+                                            d->partial.p, d->N, (int)kSplitK, t & 1, d->err.p, d->tile_cnt.p, fin));
                 continue;
             }
+            NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0)], d->stream));
             launch_delivery(d, in);
             NBG_CUDA(cudaEventRecord(d->dev_pool[2 * (k - k0) + 1], d->stream));
             k_dense_lif<<<(total + 255) / 256, 256, 0, d->stream>>>(
@@ -541,6 +549,7 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
                 tensor ? nullptr : d->bits[outp].p, dcnt.p + k, t, d->N, total);
         }
         NBG_CUDA(cudaGetLastError());
+        if (blocked) continue; // one launch per step, no per-step events (they would break the overlap)
         NBG_CUDA(cudaEventSynchronize(d->dev_pool[2 * (k1 - 1 - k0) + 1]));
         for (int k = k0; k < k1; ++k) {
             float x = 0.0f;
@@ -553,8 +562,8 @@ nbg_status nbg_dense_run(nbg_dense *d, int steps) {
     float ms = 0.0f;
     NBG_CUDA(cudaEventElapsedTime(&ms, d->ev0, d->ev1));
     d->last_ms = ms;
-    d->last_delivery_ms = dms;
-    d->last_launches = 2LL * count;
+    d->last_delivery_ms = blocked ? ms : dms; // tcgen05: the whole step is the delivery launch
+    d->last_launches = (blocked ? 1LL : 2LL) * count;
     NBG_CUDA(cudaMemcpy(cnt.data(), dcnt.p, count * sizeof(int), cudaMemcpyDeviceToHost));
     int errv = 0;
     NBG_CUDA(cudaMemcpy(&errv, d->err.p, sizeof(int), cudaMemcpyDeviceToHost));

@@ -198,15 +198,34 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    // Programmatic dependent launch: the next step's grid may be scheduled
+    // as soon as every CTA of this one has started; W does not depend on the
+    // previous step, so its first stages are requested before the grid
+    // dependency wait (a no-op without a programmatic launch), and S and all
+    // state after it.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    // K chunks in ascending order, or descending when `reverse`: the chunks a
+    // step streams last are still in L2 when the next step, run in the other
+    // direction, streams them first
+    auto chunk = [&](int it) { return reverse ? kc0 + iters - 1 - it : kc0 + it; };
     if (warp == 0 && lane == 0) { // producer: bulk copies into free stages
-        for (int it = 0; it < iters; ++it) {
+        const int pre = iters < kUStages ? iters : kUStages;
+        for (int it = 0; it < pre; ++it) {
+            uint8_t *st = stages + it * kStageBytes;
+            const size_t blk = (size_t)mt * kchunks + chunk(it);
+            mbar_expect_tx(&full[it], kStageBytes);
+            bulk_copy(st, (const uint8_t *)wt_hi + blk * kBlockA, kBlockA, &full[it]);
+            bulk_copy(st + kBlockA, (const uint8_t *)wt_lo + blk * kBlockA, kBlockA, &full[it]);
+        }
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        for (int it = 0; it < pre; ++it)
+            bulk_copy(stages + it * kStageBytes + 2 * kBlockA, (const uint8_t *)s_blk + (size_t)chunk(it) * kBlockB,
+                      kBlockB, &full[it]);
+        for (int it = pre; it < iters; ++it) {
             const int s = it % kUStages;
-            if (it >= kUStages && !mbar_wait(&empty[s], ((it / kUStages) & 1) ^ 1, abort)) break;
+            if (!mbar_wait(&empty[s], ((it / kUStages) & 1) ^ 1, abort)) break;
             uint8_t *st = stages + s * kStageBytes;
-            // K chunks in ascending order, or descending when `reverse`: the
-            // chunks a step streams last are still in L2 when the next step,
-            // run in the other direction, streams them first
-            const int kc = reverse ? kc0 + iters - 1 - it : kc0 + it;
+            const int kc = chunk(it);
             const size_t blk = (size_t)mt * kchunks + kc;
             mbar_expect_tx(&full[s], kStageBytes);
             bulk_copy(st, (const uint8_t *)wt_hi + blk * kBlockA, kBlockA, &full[s]);
@@ -235,6 +254,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         (void)issued;
     }
     __syncwarp();
+    asm volatile("griddepcontrol.wait;" ::: "memory"); // before touching anything the previous step wrote
     // epilogue: warp w reads TMEM lanes 32*(w%4).. (post neurons) and
     // columns 32*(w/4).. (instances).  The abort decision is made uniform
     // across the block before the warp-collective tcgen05.ld.
