@@ -182,6 +182,13 @@ nbg_status nbg_set_state(nbg_engine *e, int field, const float *in /* n_neurons 
 nbg_status nbg_num_spikes(nbg_engine *e, int64_t *n);
 nbg_status nbg_get_spikes(nbg_engine *e, int32_t *times, int32_t *ids, int64_t capacity);
 nbg_status nbg_clear_spikes(nbg_engine *e);
+/* The STDP decay factors the engine applies for a gap of k steps:
+ * out[k] = factor of trace `which` (0: Apre / LTP_tau, 1: Apost / LTD_tau) of
+ * rule `rule`, for k < *len (longer gaps decay to 0).  Legacy profile: host
+ * libm expf of -((float)k * dt) * (float)(1.0 / (double)tau)
+ * (STDP_State.cpp:5-26); dense profile: CUDA expf with 1.0f / max(1e-6f, tau)
+ * (DenseLearningDeviceRuntime.cuh:65-77).  Copies min(capacity, *len). */
+nbg_status nbg_get_decay_table(nbg_engine *e, int rule, int which, int64_t capacity, float *out, int64_t *len);
 /* Entries [offset, offset + count) of the recorded spikes (a monitor reading
  * only what the last run call added). */
 nbg_status nbg_get_spikes_from(nbg_engine *e, int64_t offset, int64_t count, int32_t *times, int32_t *ids);

@@ -43,6 +43,21 @@ nbg_status nbg_lif_forward_step(const float *I, float *v, int32_t *ref, float *s
                                 float *vprev_rec, float *z, float c_t, const float *alpha, const float *theta,
                                 const nbg_lif_grad_params *p, int B, int N, void *stream);
 
+/* Spike-driven forward step (spiking mode only): I_t = xi_t + the sum, in
+ * ascending neuron order, of the rows of w_rec (N x N, row = pre) listed in
+ * spk_in/cnt_in (row b's spikes of step t-1: spk_in[b*N .. b*N + cnt_in[b]]),
+ * then the step of nbg_lif_forward_step; writes row b's ascending spike list
+ * of step t to spk_out/cnt_out.  N <= 2048.  Same equations as the dense form
+ * with s_{t-1} W_rec as a gather-sum over the spikes. */
+nbg_status nbg_lif_forward_step_sparse(const float *xi, const float *w_rec, const int32_t *spk_in,
+                                       const int32_t *cnt_in, int32_t *spk_out, int32_t *cnt_out, float *v,
+                                       int32_t *ref, float *s_out, float *u_rec, uint8_t *m_rec, float *vprev_rec,
+                                       float *z, float c_t, const float *alpha, const float *theta,
+                                       const nbg_lif_grad_params *p, int B, int N, void *stream);
+
+/* Ascending spike list of every row of the 0/1 matrix s (B x N). */
+nbg_status nbg_spike_lists(const float *s, int32_t *spk, int32_t *cnt, int B, int N, void *stream);
+
 /* One adjoint step (reverse time).  g_ext may be NULL (last step). */
 nbg_status nbg_lif_adjoint_step(const float *g_ext, const float *g_read, float c_t, const float *u, const float *s,
                                 const uint8_t *m, const float *vprev, float *lam_v, float *dI, float *g_theta,

@@ -99,6 +99,8 @@ _SIGNATURES = {
     "nbg_set_weights": (ctypes.c_int, [ctypes.c_void_p, _f32p]),
     "nbg_get_spikes_from": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, _i32p, _i32p]),
     "nbg_set_layer_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "nbg_get_decay_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _f32p,
+                                           ctypes.POINTER(ctypes.c_int64)]),
     "nbg_add_external_spikes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _i32p, _i32p]),
     "nbg_add_external_currents": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _i32p, _i32p, _f32p]),
     "nbg_set_current_at": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float]),

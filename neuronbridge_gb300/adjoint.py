@@ -5,10 +5,17 @@
 time-averaged leaky readout.  Its backward is not autograd: the forward saves
 the network state every ``checkpoint`` steps, and the backward replays each
 segment from its checkpoint (recording u_t, s_t, m_t, v_{t-1}) and runs the
-fused adjoint kernel in reverse time.  Dense products go to cuBLAS through
-torch (x W_in for a whole segment at once, s W_rec and dI W_rec^T per step,
-and the weight gradients as one GEMM per segment); all elementwise work of a
-step is one CUDA kernel each way.
+fused adjoint kernel in reverse time.
+
+* x W_in (a whole segment at once), the adjoint's recurrent term
+  dI_{t+1} W_rec^T (per step) and the weight gradients (one product per
+  segment) are cuBLAS GEMMs through torch.
+* The forward recurrent input s_{t-1} W_rec: with binary spikes (spiking
+  mode) one fused kernel per step sums the W_rec rows of the previous step's
+  spikes (ascending order), runs the neuron update and writes the new spike
+  list; with sigmoid spikes it is a GEMM followed by the fused elementwise
+  step.
+* All elementwise work of an adjoint step is one fused kernel.
 
 Readout: y_t = a_out y_{t-1} + s_t W_out, a_out = exp(-dt / tau_out), and
 mean_t y_t = (sum_t c_t s_t) W_out with c_t = (1 - a_out^(T-t)) / ((1 - a_out) T),
@@ -40,6 +47,9 @@ _SIG = {
                                             _vp, ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_poisson_inputs": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                           ctypes.c_int, _vp]),
+    "nbg_lif_forward_step_sparse": (ctypes.c_int, [_vp] * 13 + [ctypes.c_float, _vp, _vp, ctypes.POINTER(GradParams),
+                                                                ctypes.c_int, ctypes.c_int, _vp]),
+    "nbg_spike_lists": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
 }
 _LIB = None
 
@@ -78,11 +88,38 @@ def readout_coefficients(T: int, a_out: float) -> np.ndarray:
     return ((1.0 - a_out ** (T - t)) / ((1.0 - a_out) * T)).astype(np.float32)
 
 
+class _SpikeLists:
+    """Double-buffered ascending spike lists of the B rows (spiking mode): the
+    recurrent input s_{t-1} W_rec is a gather-sum over them."""
+
+    def __init__(self, B: int, N: int, device):
+        self.idx = torch.empty((2, B, N), device=device, dtype=torch.int32)
+        self.cnt = torch.zeros((2, B), device=device, dtype=torch.int32)
+        self.cur = 0
+
+    def load(self, lib, s, B, N, st):
+        _lib.check(lib.nbg_spike_lists(_ptr(s), _ptr(self.idx[self.cur]), _ptr(self.cnt[self.cur]), B, N, st))
+
+    def step(self, lib, xi, w_rec, v, ref, s_out, u_rec, m_rec, vp_rec, z, c, alpha, theta, p, B, N, st):
+        a, b = self.cur, self.cur ^ 1
+        _lib.check(lib.nbg_lif_forward_step_sparse(
+            _ptr(xi), _ptr(w_rec), _ptr(self.idx[a]), _ptr(self.cnt[a]), _ptr(self.idx[b]), _ptr(self.cnt[b]),
+            _ptr(v), _ptr(ref), _ptr(s_out), _ptr(u_rec), _ptr(m_rec), _ptr(vp_rec), _ptr(z), float(c), _ptr(alpha),
+            _ptr(theta), ctypes.byref(p), B, N, st))
+        self.cur = b
+
+
+def _sparse_ok(p, N: int) -> bool:
+    return not p.smooth and N <= 2048
+
+
 def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out):
     """Forward recurrence into caller-owned buffers: the checkpoints
     ck_*[segment] (state entering each K-step segment), the readout
     accumulator z and the output z W_out.  Launches only (no host sync), so it
-    runs eagerly or under CUDA graph capture alike."""
+    runs eagerly or under CUDA graph capture alike.  With binary spikes the
+    recurrent product is the spike-driven gather-sum (one fused kernel per
+    step); with sigmoid spikes it is a GEMM."""
     T, B, C = x.shape
     N = w_rec.shape[0]
     st = _stream()
@@ -92,6 +129,8 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
     s_prev = sbuf[1]
     s_prev.zero_()
     z.zero_()
+    sparse = _sparse_ok(p, N)
+    lists = _SpikeLists(B, N, x.device) if sparse else None  # no spikes before step 0
     I = torch.empty((B, N), device=x.device, dtype=torch.float32)
     for seg, t0 in enumerate(range(0, T, K)):
         t1 = min(T, t0 + K)
@@ -100,10 +139,14 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
         ck_s[seg].copy_(s_prev)
         xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
         for t in range(t0, t1):
-            torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
             s = sbuf[t & 1]
-            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
-                                                float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
+            if sparse:
+                lists.step(lib, xi[t - t0], w_rec, v, ref, s, None, None, None, z, coef[t], alpha, theta, p, B, N, st)
+            else:
+                torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
+                _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
+                                                    float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N,
+                                                    st))
             s_prev = s
     torch.mm(z, w_out, out=out)
 
@@ -133,6 +176,8 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     dI = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
     dI_next = torch.empty((B, N), device=x.device, dtype=torch.float32)
     have_next = False
+    sparse = _sparse_ok(p, N)
+    lists = _SpikeLists(B, N, x.device) if sparse else None
     segments = list(enumerate(range(0, T, K)))
     for seg, t0 in reversed(segments):
         t1 = min(T, t0 + K)
@@ -140,7 +185,13 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         v, ref = ck_v[seg].clone(), ck_ref[seg].clone()
         S[0].copy_(ck_s[seg])
         xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
+        if sparse:
+            lists.load(lib, S[0], B, N, st)
         for k in range(L):
+            if sparse:
+                lists.step(lib, xi[k], w_rec, v, ref, S[k + 1], U[k], M[k], VP[k], None, 0.0, alpha, theta, p, B, N,
+                           st)
+                continue
             torch.addmm(xi[k], S[k], w_rec, out=I)
             _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
                                                 _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
@@ -148,7 +199,7 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         for k in reversed(range(L)):
             t = t0 + k
             ge = None
-            if have_next:
+            if have_next:  # dL/ds_t from the recurrent path: dI_{t+1} W_rec^T
                 torch.mm(dI_next if k == L - 1 else dI[k + 1], w_rec.t(), out=g_ext)
                 ge = g_ext
             _lib.check(lib.nbg_lif_adjoint_step(_ptr(ge), _ptr(g_read), float(coef[t]), _ptr(U[k]),

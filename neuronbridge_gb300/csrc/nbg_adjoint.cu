@@ -68,6 +68,115 @@ __global__ void __launch_bounds__(256) k_lif_adj(const float *__restrict__ g_ext
     g_alpha[idx] = g_alpha[idx] + gm * (p.v_rest - vprev[idx]);
 }
 
+// Spike-driven forward step (spiking mode, binary s): one CTA per instance
+// row b.  I = xi + the sum of the W_rec rows of the previous step's spikes in
+// ascending neuron order (the spike list of row b), then the same update as
+// k_lif_fwd, then the row's new spike list in ascending order (block-wide
+// ballot prefix).  Each thread owns columns j = threadIdx.x + q * blockDim.x.
+constexpr int kSparseThreads = 256;
+constexpr int kSparseCols = 8; // columns per thread: N <= 2048
+
+__global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_sparse(
+    const float *__restrict__ xi, const float *__restrict__ w, const int *__restrict__ idx_in,
+    const int *__restrict__ cnt_in, int *__restrict__ idx_out, int *__restrict__ cnt_out, float *__restrict__ v,
+    int *__restrict__ ref, float *__restrict__ s_out, float *__restrict__ u_rec, unsigned char *__restrict__ m_rec,
+    float *__restrict__ vprev_rec, float *__restrict__ z, float c_t, const float *__restrict__ alpha,
+    const float *__restrict__ theta, nbg_lif_grad_params p, int N) {
+    __shared__ int warp_base[kSparseThreads / 32 + 1];
+    const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const size_t row = (size_t)b * N;
+    const int nq = (N + kSparseThreads - 1) / kSparseThreads;
+    float acc[kSparseCols];
+#pragma unroll
+    for (int q = 0; q < kSparseCols; ++q) {
+        const int j = tid + q * kSparseThreads;
+        acc[q] = (q < nq && j < N) ? xi[row + j] : 0.0f;
+    }
+    const int cnt = cnt_in[b];
+    const int *list = idx_in + row;
+    for (int k = 0; k < cnt; ++k) {
+        const float *wr = w + (size_t)__ldg(&list[k]) * N;
+#pragma unroll
+        for (int q = 0; q < kSparseCols; ++q) {
+            const int j = tid + q * kSparseThreads;
+            if (q < nq && j < N) acc[q] = acc[q] + __ldg(&wr[j]);
+        }
+    }
+    int base = 0; // spikes of this row in earlier column chunks
+    for (int q = 0; q < nq; ++q) {
+        const int j = tid + q * kSparseThreads;
+        bool spk = false;
+        if (j < N) {
+            const size_t i = row + j;
+            const float vp = v[i];
+            const int rf = ref[i];
+            const bool m = rf == 0;
+            float a_q = acc[0];
+#pragma unroll
+            for (int r = 1; r < kSparseCols; ++r)
+                if (q == r) a_q = acc[r];
+            const float u = m ? vp + alpha[j] * (p.v_rest - vp) + a_q : p.v_reset;
+            const float sv = u > theta[j] ? 1.0f : 0.0f;
+            v[i] = u - sv * (u - p.v_reset);
+            ref[i] = sv > 0.0f ? p.t_ref : (rf > 0 ? rf - 1 : 0);
+            s_out[i] = sv;
+            if (u_rec) u_rec[i] = u;
+            if (m_rec) m_rec[i] = m ? 1 : 0;
+            if (vprev_rec) vprev_rec[i] = vp;
+            if (z) z[i] = z[i] + c_t * sv;
+            spk = sv > 0.0f;
+        }
+        // ordered compaction of this chunk's spikes
+        const unsigned bal = __ballot_sync(0xffffffffu, spk);
+        if (lane == 0) warp_base[wid] = __popc(bal);
+        __syncthreads();
+        if (tid == 0) {
+            int sum = 0;
+            for (int k = 0; k < kSparseThreads / 32; ++k) {
+                const int c = warp_base[k];
+                warp_base[k] = sum;
+                sum += c;
+            }
+            warp_base[kSparseThreads / 32] = sum;
+        }
+        __syncthreads();
+        if (spk) idx_out[row + base + warp_base[wid] + __popc(bal & ((1u << lane) - 1u))] = j;
+        base += warp_base[kSparseThreads / 32];
+        __syncthreads();
+    }
+    if (tid == 0) cnt_out[b] = base;
+}
+
+// Ascending spike list of each row of a 0/1 matrix (segment restarts).
+__global__ void __launch_bounds__(kSparseThreads) k_spike_list(const float *__restrict__ s, int *__restrict__ idx,
+                                                               int *__restrict__ cnt, int N) {
+    __shared__ int warp_base[kSparseThreads / 32 + 1];
+    const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const size_t row = (size_t)b * N;
+    int base = 0;
+    for (int c0 = 0; c0 < N; c0 += kSparseThreads) {
+        const int j = c0 + tid;
+        const bool spk = j < N && s[row + j] > 0.0f;
+        const unsigned bal = __ballot_sync(0xffffffffu, spk);
+        if (lane == 0) warp_base[wid] = __popc(bal);
+        __syncthreads();
+        if (tid == 0) {
+            int sum = 0;
+            for (int k = 0; k < kSparseThreads / 32; ++k) {
+                const int c = warp_base[k];
+                warp_base[k] = sum;
+                sum += c;
+            }
+            warp_base[kSparseThreads / 32] = sum;
+        }
+        __syncthreads();
+        if (spk) idx[row + base + warp_base[wid] + __popc(bal & ((1u << lane) - 1u))] = j;
+        base += warp_base[kSparseThreads / 32];
+        __syncthreads();
+    }
+    if (tid == 0) cnt[b] = base;
+}
+
 __global__ void k_poisson(float *__restrict__ x, const float *__restrict__ rates, int T, int B, int C, float dt,
                           int seed, long long total) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,6 +217,32 @@ nbg_status nbg_lif_adjoint_step(const float *g_ext, const float *g_read, float c
     const int total = B * N;
     k_lif_adj<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(g_ext, g_read, c_t, u, s, m, vprev, lam_v, dI,
                                                                       g_theta, g_alpha, alpha, theta, *p, N, total);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_lif_forward_step_sparse(const float *xi, const float *w_rec, const int32_t *spk_in,
+                                       const int32_t *cnt_in, int32_t *spk_out, int32_t *cnt_out, float *v,
+                                       int32_t *ref, float *s_out, float *u_rec, uint8_t *m_rec, float *vprev_rec,
+                                       float *z, float c_t, const float *alpha, const float *theta,
+                                       const nbg_lif_grad_params *p, int B, int N, void *stream) {
+    if (!xi || !w_rec || !spk_in || !cnt_in || !spk_out || !cnt_out || !v || !ref || !s_out || !alpha || !theta ||
+        !p || B <= 0 || N <= 0)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_forward_step_sparse: bad arguments");
+    if (p->smooth) return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step needs binary spikes (smooth = 0)");
+    if (N > kSparseThreads * kSparseCols)
+        return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step supports up to %d neurons",
+                        kSparseThreads * kSparseCols);
+    k_lif_fwd_sparse<<<B, kSparseThreads, 0, (cudaStream_t)stream>>>(xi, w_rec, spk_in, cnt_in, spk_out, cnt_out, v,
+                                                                      ref, s_out, u_rec, m_rec, vprev_rec, z, c_t,
+                                                                      alpha, theta, *p, N);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_spike_lists(const float *s, int32_t *spk, int32_t *cnt, int B, int N, void *stream) {
+    if (!s || !spk || !cnt || B <= 0 || N <= 0) return nbg_fail(NBG_ERR_INVALID, "nbg_spike_lists: bad arguments");
+    k_spike_list<<<B, kSparseThreads, 0, (cudaStream_t)stream>>>(s, spk, cnt, N);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

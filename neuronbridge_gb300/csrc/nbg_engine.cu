@@ -831,6 +831,8 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
 
 } // namespace
 
+NBG_HIDDEN cudaError_t nbg_device_decay_table(float *tab, const float *inv_host, int rows, int len, float dt);
+
 struct nbg_engine {
     int device = 0;
     int N = 0;
@@ -978,9 +980,40 @@ namespace {
 
 // Host decay table: table[k] = expf(-((float)k * dt) * inv_tau), the exact
 // float expression of STDP_State::SetUpdate evaluated with the host libm.
+// Dense-runtime profile: the table is built on the device with CUDA's expf
+// and inv_tau = 1.0f / max(1e-6f, tau) (DenseStdpLearningModel.h:115,
+// DenseLearningDeviceRuntime.cuh:65-77), long enough that its last entry is
+// 0 (expf of an argument below -104 is 0 in float).
+nbg_status dense_decay_table(nbg_engine *e) {
+    std::vector<float> inv((size_t)e->n_rules * 2);
+    int64_t len = 1;
+    for (int r = 0; r < e->n_rules; ++r) {
+        inv[r * 2 + 0] = 1.0f / std::max(1.0e-6f, e->rules[r].ltp_tau);
+        inv[r * 2 + 1] = 1.0f / std::max(1.0e-6f, e->rules[r].ltd_tau);
+        for (int w = 0; w < 2; ++w) {
+            int64_t k = 1;
+            while ((float)k * e->dt * inv[r * 2 + w] <= 104.0f && k < ((int64_t)1 << 24)) k *= 2;
+            len = std::max(len, k + 1);
+        }
+    }
+    if (len > ((int64_t)1 << 24)) return fail(NBG_ERR_UNSUPPORTED, "STDP decay table would exceed 2^24 entries");
+    NBG_CUDA(e->dtab.alloc((size_t)e->n_rules * 2 * len));
+    NBG_CUDA(nbg_device_decay_table(e->dtab.p, inv.data(), e->n_rules * 2, (int)len, e->dt));
+    e->dtab_len = (int)len;
+    e->dtab_complete = true;
+    for (int row = 0; row < e->n_rules * 2; ++row) { // verify the underflow to 0
+        float last = 1.0f;
+        NBG_CUDA(cudaMemcpy(&last, e->dtab.p + (size_t)row * len + len - 1, sizeof(float), cudaMemcpyDeviceToHost));
+        if (last != 0.0f) e->dtab_complete = false;
+    }
+    if (!e->dtab_complete) return fail(NBG_ERR_UNSUPPORTED, "dense STDP decay table did not reach 0");
+    return NBG_OK;
+}
+
 nbg_status ensure_decay_table(nbg_engine *e, int64_t needed) {
     if (e->n_rules == 0) return NBG_OK;
     if (e->dtab_complete || e->dtab_len >= needed) return NBG_OK;
+    if (e->semantics == NBG_SEM_DENSE) return dense_decay_table(e);
     int64_t len = std::max<int64_t>(needed, 4096);
     len = std::min<int64_t>(len, (int64_t)1 << 24);
     std::vector<float> tab((size_t)e->n_rules * 2 * len);
@@ -1811,6 +1844,22 @@ nbg_status nbg_set_layer_record(nbg_engine *e, int layer, int record) {
     NBG_CUDA(cudaStreamSynchronize(e->stream));
     e->layers[layer].record = record != 0 ? 1 : 0;
     NBG_CUDA(cudaMemcpy(e->d_layers.p + layer, &e->layers[layer], sizeof(LayerDev), cudaMemcpyHostToDevice));
+    return NBG_OK;
+}
+
+nbg_status nbg_get_decay_table(nbg_engine *e, int rule, int which, int64_t capacity, float *out, int64_t *len) {
+    if (!e || !len) return fail(NBG_ERR_INVALID, "null argument");
+    if (rule < 0 || rule >= e->n_rules || which < 0 || which > 1)
+        return fail(NBG_ERR_INVALID, "no decay table (rule %d, trace %d)", rule, which);
+    nbg_status st = ensure_decay_table(e, 1);
+    if (st != NBG_OK) return st;
+    *len = e->dtab_len;
+    if (out && capacity > 0) {
+        NBG_CUDA(cudaSetDevice(e->device));
+        const int64_t n = std::min<int64_t>(capacity, e->dtab_len);
+        NBG_CUDA(cudaMemcpy(out, e->dtab.p + (size_t)(rule * 2 + which) * e->dtab_len, n * sizeof(float),
+                            cudaMemcpyDeviceToHost));
+    }
     return NBG_OK;
 }
 

@@ -87,6 +87,7 @@ def _lib(prec: int):
             "set_threads": (None, [vp, ctypes.c_int]),
             "add_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             "add_external_spike": (None, [vp, ctypes.c_int, ctypes.c_int]),
+            "set_decay_table": (None, [vp, ctypes.c_int64, f32p]),
             "add_external_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             "dense_create": (vp, [ctypes.c_int, ctypes.c_int, f32p, f32p, i32p, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float]),
@@ -205,6 +206,14 @@ class OracleNet:
     def add_current(self, t: int, neuron: int, value: float) -> None:
         """Set neuron's external current to ``value`` at the start of step t."""
         self._f("add_current")(self.h, int(t), int(neuron), float(value))
+
+    def set_decay_table(self, table) -> "OracleNet":
+        """Use the given STDP decay factors ([rule][2][len] float32) instead of
+        expf: the dense-runtime profile's factors come from CUDA's expf."""
+        tab = np.ascontiguousarray(table, np.float32)
+        self._keep["dtab"] = tab
+        self._f("set_decay_table")(self.h, int(tab.shape[-1]), _ptr(tab, ctypes.c_float))
+        return self
 
     def add_external_spikes(self, times, neurons) -> "OracleNet":
         """InputSpike events: each neuron spikes at its step."""

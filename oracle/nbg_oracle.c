@@ -136,6 +136,11 @@ typedef struct {
     REAL *lat_v;
     int64_t lat_vcap;
     REAL *latch; /* per CSC position (only current synapses used) */
+    /* decay factors supplied by the caller ([rule][2][len], factor of a gap of
+     * k steps; longer gaps decay to 0): the dense-runtime profile's factors
+     * come from CUDA's expf, which this file does not restate */
+    float *dtab_ext;
+    int64_t dtab_ext_len;
     int threads;          /* OpenMP threads for the per-step loops (1 = serial) */
     unsigned char *fired; /* per-neuron spike flags of the current update */
     int64_t *seg;         /* target segment starts of the sorted bucket */
@@ -433,6 +438,7 @@ void ORC(destroy)(void *hp) {
     free(n->lat_p.v);
     free(n->lat_v);
     free(n->latch);
+    free(n->dtab_ext);
     free(n->fired);
     free(n->seg);
     free(n);
@@ -442,7 +448,13 @@ void ORC(destroy)(void *hp) {
  * deltaTime = (float)(t - last) * dt; A *= exp(-deltaTime * inv_tau). */
 static void stdp_decay(net_t *n, int64_t p, int t) {
     int r = n->csc_rule[p];
-    if (sizeof(REAL) == sizeof(float)) {
+    if (n->dtab_ext) {
+        int64_t gap = (int64_t)t - n->slast[p];
+        float fp = gap < n->dtab_ext_len ? n->dtab_ext[(size_t)(r * 2 + 0) * n->dtab_ext_len + gap] : 0.0f;
+        float fm = gap < n->dtab_ext_len ? n->dtab_ext[(size_t)(r * 2 + 1) * n->dtab_ext_len + gap] : 0.0f;
+        n->apre[p] *= (REAL)fp;
+        n->apost[p] *= (REAL)fm;
+    } else if (sizeof(REAL) == sizeof(float)) {
         float dtime = (float)(t - n->slast[p]) * n->dt_f;
         n->apre[p] *= (REAL)expf(-dtime * (float)n->inv_ltp[r]);
         n->apost[p] *= (REAL)expf(-dtime * (float)n->inv_ltd[r]);
@@ -882,6 +894,18 @@ void ORC(get_events)(void *hp, int *t, int64_t *conn, double *w) {
         conn[k] = n->csc_orig[n->ev_pos.v[k]];
         w[k] = (double)n->ev_w[k];
     }
+}
+
+void ORC(set_decay_table)(void *hp, int64_t len, const float *vals) {
+    net_t *n = (net_t *)hp;
+    free(n->dtab_ext);
+    n->dtab_ext = NULL;
+    n->dtab_ext_len = 0;
+    if (len <= 0 || !vals) return;
+    size_t count = (size_t)(n->n_rules > 0 ? n->n_rules : 1) * 2 * (size_t)len;
+    n->dtab_ext = (float *)malloc(count * sizeof(float));
+    memcpy(n->dtab_ext, vals, count * sizeof(float));
+    n->dtab_ext_len = len;
 }
 
 void ORC(add_external_spike)(void *hp, int t, int id) {

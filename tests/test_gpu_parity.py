@@ -8,11 +8,13 @@ operation matches.  Size-independent properties (determinism, composition of
 run calls, invariance to launch shape, instance independence in a batch) are
 checked at larger sizes.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
 import neuronbridge_gb300 as nb
-from neuronbridge_gb300 import workloads
+from neuronbridge_gb300 import _lib, workloads
 
 pytestmark = pytest.mark.gpu
 
@@ -279,3 +281,39 @@ def test_nbnet_path_simulation_equals_in_memory(tmp_path, oracle_lib):
     assert _raster_equal(a.spike_raster(), b.spike_raster())
     assert np.array_equal(a.weights()["weight"], b.weights()["weight"])
     assert np.array_equal(a.state_field(0), b.state_field(0))
+
+
+def _decay_table(sim, rules):
+    n = ctypes.c_int64()
+    _lib.check(sim.lib.nbg_get_decay_table(sim._h, 0, 0, 0, None, ctypes.byref(n)))
+    tab = np.zeros((rules, 2, n.value), np.float32)
+    for r in range(rules):
+        for w in range(2):
+            _lib.check(sim.lib.nbg_get_decay_table(sim._h, r, w, n.value,
+                                                   tab[r, w].ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                   ctypes.byref(n)))
+    return tab
+
+
+def test_dense_profile_stdp_uses_device_expf(oracle_lib):
+    """Dense-runtime STDP: decay factors from CUDA's expf with
+    inv_tau = 1/max(1e-6, tau) (DenseLearningDeviceRuntime.cuh:65-77), built
+    on the device; the oracle, given the same factors, is bit-exact.  The
+    factors stay within 2 ulp of the host libm table of the legacy profile
+    (CUDA documents a 2-ulp bound for expf)."""
+    import oracle
+
+    net, cfg = workloads.izhikevich_stdp(n=2000, in_degree=50)
+    dense = nb.Simulation(net, cfg, seed=2, semantics="dense")
+    legacy = nb.Simulation(net, cfg, seed=2)
+    td, tl = _decay_table(dense, 1), _decay_table(legacy, 1)
+    n = min(td.shape[-1], tl.shape[-1])
+    ulp = np.abs(td[..., :n].view(np.int32).astype(np.int64) - tl[..., :n].view(np.int32).astype(np.int64))
+    assert ulp.max() <= 2 and td[..., -1].max() == 0.0
+    dense.run(1500)
+    o = oracle.OracleNet(net.to_native().flat(cfg.timestep, semantics=1, seed=2))
+    o.set_decay_table(td)
+    o.run(1500)
+    assert _raster_equal(dense.spike_raster(), _oracle_raster(o, net))
+    assert np.array_equal(dense.weights()["weight"], o.weights()[0].astype(np.float32))
+    assert not np.array_equal(dense.weights()["weight"], net.to_native().weight)
