@@ -57,6 +57,9 @@ BYTES_PER_POST_UPDATE = 36
 # DRAM bytes (read + write) of one k_update launch of this workload (10 steps x
 # 100k neurons) from an ncu capture of that launch with a cold L2
 KUPDATE_TRAFFIC_BYTES = 80.6e6
+# DRAM bytes (read + write) of one dense step launch (64 x 8192, delivery and
+# update) from an ncu capture with a cold L2
+DENSE_TRAFFIC_BYTES = 277.5e6
 
 
 def _peaks():
@@ -333,9 +336,12 @@ def bench_dense(args) -> dict:
     return _common(args, "steps/s", 1e3 / sp["ms_per_step"], "steps/s", sp["ms_per_step"] * per,
                    {"workload": "dense_split_bf16_64x8192", "instances": 64, "neurons": n, "sim_steps_per_step": per},
                    neuron_steps_per_s=64 * n * 1e3 / sp["ms_per_step"],
-                   roofline={"bound": "hbm", "kernel": "k_dense_umma (split BF16, tcgen05)", "achieved": achieved,
-                             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": kind,
-                             "traffic": None, "tflops": flops / (sp["delivery_us"] * 1e-6) / 1e12},
+                   roofline={"bound": "hbm", "kernel": "k_dense_umma<LifFinish> (split-BF16 delivery + LIF, tcgen05)",
+                             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "peak_kind": kind, "traffic": DENSE_TRAFFIC_BYTES if n == 8192 else None,
+                             "traffic_unit": "bytes per launch (ncu, cold L2, one step)",
+                             "algorithmic_bytes_per_launch": byts,
+                             "tflops": flops / (sp["delivery_us"] * 1e-6) / 1e12},
                    paths=out)
 
 
