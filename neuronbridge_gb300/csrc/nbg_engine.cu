@@ -221,6 +221,23 @@ __device__ __forceinline__ Model load_model(const LayerDev &L) {
     return m;
 }
 
+// Compile-time network profile of an update-kernel instance: the neuron
+// models that may occur (bit m = model m) and whether synapses learn
+// (1 yes, 0 no, -1 decided per launch from the STDP arrays).  With one model
+// the per-neuron dispatch folds away; without learning the STDP loads and
+// the post-synaptic pass are not compiled.
+template <unsigned kModels, int kPlastic>
+struct Spec {
+    static constexpr bool has(int m) { return (kModels >> m) & 1u; }
+    static constexpr int single() {
+        return (kModels != 0u && (kModels & (kModels - 1u)) == 0u) ? __builtin_ctz(kModels) : -1;
+    }
+    __device__ static int model(int m) { return single() >= 0 ? single() : m; }
+    __device__ static bool plastic(const NetDev &n) { return kPlastic < 0 ? n.apre != nullptr : kPlastic > 0; }
+};
+constexpr unsigned kAllModels = 0x3fu;
+using GenericSpec = Spec<kAllModels, -1>;
+
 __device__ __forceinline__ float clamp_w(float w, float wmax) {
     if (w < 0.0f) return 0.0f;
     if (w > wmax) return wmax;
@@ -295,36 +312,41 @@ __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, i
 // weight as it is before this step's pre hook, then the pre hook if the
 // synapse is plastic.  The STDP state is loaded speculatively together with
 // meta and weight (one memory round trip), then the decay-table entry.
+template <class S>
 __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
                                               float &acc_b, bool gate, int s, int t) {
     const unsigned char meta = n.meta[s];
     const float w = n.w[s];
     int last = 0;
     float apre = 0.0f, apost = 0.0f, wmax = 0.0f;
-    if (n.apre) { // the network has plastic synapses: state arrays exist for every synapse
+    if (S::plastic(n)) { // the network has plastic synapses: state arrays exist for every synapse
         last = n.slast[s];
         apre = n.apre[s];
         apost = n.apost[s];
         wmax = n.wmax[s];
     }
     const int type = meta & 1;
-    switch (M.model) {
+    switch (S::model(M.model)) {
     case NBG_MODEL_LIF_VJ:
-        if (n.semantics == NBG_SEM_DENSE) {
-            if (type == 0) acc_a = acc_a + w;
-            else acc_b = acc_b + w;
-        } else if (gate) {
-            r.v = r.v + (type ? -w : w);
+        if constexpr (S::has(NBG_MODEL_LIF_VJ)) {
+            if (n.semantics == NBG_SEM_DENSE) {
+                if (type == 0) acc_a = acc_a + w;
+                else acc_b = acc_b + w;
+            } else if (gate) {
+                r.v = r.v + (type ? -w : w);
+            }
         }
         break;
     case NBG_MODEL_IZH_COND:
-        if (n.semantics == NBG_SEM_DENSE) { // summed into the step's pending channels
-            if (type == 0) acc_a = acc_a + w;
-            else acc_b = acc_b + w;
-        } else if (type == 0) {
-            r.gexc = r.gexc + w;
-        } else {
-            r.ginh = r.ginh + w;
+        if constexpr (S::has(NBG_MODEL_IZH_COND)) {
+            if (n.semantics == NBG_SEM_DENSE) { // summed into the step's pending channels
+                if (type == 0) acc_a = acc_a + w;
+                else acc_b = acc_b + w;
+            } else if (type == 0) {
+                r.gexc = r.gexc + w;
+            } else {
+                r.ginh = r.ginh + w;
+            }
         }
         break;
     case NBG_MODEL_INPUT_SPIKE:
@@ -344,7 +366,7 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, N
             atomicOr(n.err, kErrEventLog);
         }
     }
-    if (meta >= 2) { // pre-synaptic pair STDP (STDP::ApplyPreSynaticSpike)
+    if (S::plastic(n) && meta >= 2) { // pre-synaptic pair STDP (STDP::ApplyPreSynaticSpike)
         const int rule = (int)(meta >> 1) - 1;
         const int gap = t - last;
         float fp = 0.0f, fm = 0.0f;
@@ -363,6 +385,7 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, N
 
 // Apply every set bit of `word` (word index wi of this target) in ascending
 // order.
+template <class S>
 __device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
                                            float &acc_b, bool gate, unsigned int word, int first, int t) {
     while (word) {
@@ -373,7 +396,7 @@ __device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, Neur
             if (word) {
                 sp[k] = first + __ffs(word) - 1;
                 word &= word - 1u;
-                apply_arrival(n, M, r, acc_a, acc_b, gate, sp[k], t);
+                apply_arrival<S>(n, M, r, acc_a, acc_b, gate, sp[k], t);
             }
         }
     }
@@ -396,10 +419,12 @@ __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, i
 
 // One neuron update; returns true on a spike.  `noise` is
 // sigma * gauss12(noise_key(seed, j), t) for noisy IZH_RK4 layers (else 0).
+template <class S>
 __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, NeuronRegs &r, float acc_a,
                                              float acc_b, float noise, int j, int t) {
-    switch (M.model) {
+    switch (S::model(M.model)) {
     case NBG_MODEL_LIF_VJ: {
+        if constexpr (!S::has(NBG_MODEL_LIF_VJ)) return false;
         if (n.semantics == NBG_SEM_DENSE) {
             float nv = r.v + acc_a - acc_b;
             if (r.last >= M.ip) nv = nv + M.p[5] * (M.p[0] - nv + M.p[3] * r.iext);
@@ -425,6 +450,7 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
         return false;
     }
     case NBG_MODEL_IZH_COND: {
+        if constexpr (!S::has(NBG_MODEL_IZH_COND)) return false;
         if (n.semantics == NBG_SEM_DENSE) {
             // dense runtime (DenseIzhikevichExponentialDecayDeviceUpdate.cuh:10-68):
             // decay-then-add conductances, u from the new v, no refractory gate
@@ -472,6 +498,7 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
         return false;
     }
     case NBG_MODEL_IZH_RK4: {
+        if constexpr (!S::has(NBG_MODEL_IZH_RK4)) return false;
         const float a = M.p[0], b = M.p[1];
         float I = acc_a + r.iext;
         if (M.p[5] != 0.0f) I = I + noise;
@@ -501,6 +528,7 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
     case NBG_MODEL_INPUT_CURRENT: // no time-driven dynamics
         return false;
     default: { // POISSON
+        if constexpr (!S::has(NBG_MODEL_POISSON)) return false;
         float rate = M.p[0] + acc_a + M.p[1] * r.iext;
         rate = rate > 0.0f ? rate : 0.0f;
         float prob = rate * n.dt * 0.001f;
@@ -595,6 +623,7 @@ __device__ __forceinline__ void mark_out(const NetDev &n, int q, int q1, unsigne
 }
 
 // One block of B steps starting toff steps after the run call's first step.
+template <class S>
 __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B, int toff) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = j < n.N;
@@ -650,7 +679,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
         }
     }
     // noisy RK4 neurons: per-neuron noise key (the per-step draw is made in the step loop)
-    const bool noisy = active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f;
+    const bool noisy = S::has(NBG_MODEL_IZH_RK4) && active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f;
     const unsigned int nkey = noisy ? noise_key(n.seed, j) : 0u;
     // Fast path (in-degree <= 1024, <= 32 generator inputs): the L2-resident
     // word summary says which of this neuron's mask words hold arrivals, so
@@ -733,7 +762,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
                         if ((gp >> 5) == wi) word |= 1u << (gp & 31);
                     }
                     delivered += __popc(word);
-                    apply_word(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
+                    apply_word<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
                 }
             } else {
                 int gq = g0;
@@ -745,18 +774,18 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
                             word |= 1u << (n.gen_pos[gq] & 31);
                     if (!word) continue;
                     delivered += __popc(word);
-                    apply_word(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
+                    apply_word<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
                 }
                 // this neuron's summary bits (set while its words were non-zero)
                 summary_clear_range(n.wsum + (size_t)slot * n.Ws, woff, nw);
             }
-            spk = update_neuron(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
+            spk = update_neuron<S>(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
         }
         if (spk) spk_steps |= 1u << b;
         // post-synaptic STDP (STDP::ApplyPostSynaticSpike) of every spiking
         // lane, the warp striding over that neuron's in-synapses
-        unsigned int sbal = __ballot_sync(0xffffffffu, spk && end > base);
+        unsigned int sbal = S::plastic(n) ? __ballot_sync(0xffffffffu, spk && end > base) : 0u;
         while (sbal) {
             const int l = __ffs(sbal) - 1;
             sbal &= sbal - 1u;
@@ -841,6 +870,7 @@ struct nbg_engine {
     int threads = 256;
     int n_rules = 0;
     bool plastic = false; // any synapse with a learning rule
+    void (*update_kernel)(NetDev, int, int) = nullptr; // k_update instance for this network's profile
     float dt = 1.0f;
     int semantics = 0;
     unsigned long long seed = 0;
@@ -1109,7 +1139,7 @@ void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int slot, bo
     const int grid = (e->N + e->threads - 1) / e->threads;
     const unsigned int flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 0], e->stream, flags);
-    k_update<<<grid, e->threads, 0, e->stream>>>(nd, B, toff);
+    e->update_kernel<<<grid, e->threads, 0, e->stream>>>(nd, B, toff);
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 1], e->stream, flags);
 }
 
@@ -1412,6 +1442,17 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     }
     if ((uint64_t)e->Wt * 32ull > 0xFFFFFFFFull) return bail(fail(NBG_ERR_UNSUPPORTED, "too many synapses"));
 
+    {   // update-kernel instance: the models present and whether anything learns
+        unsigned models = 0u;
+        for (const LayerDev &L : e->layers) models |= 1u << L.model;
+        const unsigned lif_poisson = (1u << NBG_MODEL_LIF_VJ) | (1u << NBG_MODEL_POISSON);
+        if (models == (1u << NBG_MODEL_IZH_RK4) && e->plastic)
+            e->update_kernel = k_update<Spec<1u << NBG_MODEL_IZH_RK4, 1>>;
+        else if ((models & ~lif_poisson) == 0u && !e->plastic)
+            e->update_kernel = k_update<Spec<lif_poisson, 0>>;
+        else
+            e->update_kernel = k_update<GenericSpec>;
+    }
     int B = opt.block_steps > 0 ? std::min(opt.block_steps, e->dmin) : e->dmin;
     e->B = std::max(1, std::min(B, kMaxBlockSteps));
 
