@@ -197,7 +197,10 @@ def bench_lif(args) -> dict:
     from neuronbridge_gb300 import tuning, workloads
 
     net, cfg = workloads.plain_lif()
-    sim = nb.Simulation(net, cfg, kernel_timing=True)
+    # no per-launch events: they would sit between the launches of the graph
+    # and stretch it; the only kernel of the call is k_update, so the call's
+    # device time over its launches is the launch duration
+    sim = nb.Simulation(net, cfg)
     tune = tuning.autotune(sim, trial_steps=1000)  # launch shape only; resets the simulation
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
@@ -214,7 +217,7 @@ def bench_lif(args) -> dict:
         p = sim.bench_profiling_snapshot()
         ev += sim.num_events - e0
         dev += p["device_ms"] / 1e3
-        upd += p["update_kernel_ms"] / 1e3
+        upd += p["device_ms"] / 1e3
         launches += p["kernel_launches"]
         sim.clear_spikes()
         flush.fill_(1.0)
@@ -242,7 +245,7 @@ def bench_batched(args) -> dict:
     t0 = time.perf_counter()
     singles, union, cfg = workloads.batched_lif()
     build_s = time.perf_counter() - t0
-    sim = nb.Simulation(union, cfg, kernel_timing=True)
+    sim = nb.Simulation(union, cfg)
     tune = tuning.autotune(sim, trial_steps=300)
     for _ in range(args.warmup):
         sim.run(cfg.steps)
@@ -428,7 +431,11 @@ def main() -> None:
 
     net, cfg = workloads.izhikevich_stdp()
     desc = net.to_native()
-    sim = nb.Simulation(desc, cfg, device=local, seed=2, kernel_timing=True)
+    # no per-launch events (they would sit between the graph's launches and
+    # stretch it): k_update is the only kernel of a run call, so the call's
+    # device time (CUDA events on the engine stream) over its launch count is
+    # the average launch duration
+    sim = nb.Simulation(desc, cfg, device=local, seed=2)
     tune = tuning.autotune(sim, trial_steps=500)  # launch shape only; resets the simulation
     fan = _post_fanout(desc)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -460,7 +467,7 @@ def main() -> None:
         tot_ev += ev
         tot_wall += wall
         tot_dev += prof["device_ms"] / 1e3
-        tot_upd += prof["update_kernel_ms"] / 1e3
+        tot_upd += prof["device_ms"] / 1e3
         tot_spk += nspk
         tot_post += int(fan[new_ids].sum())
         launches += prof["kernel_launches"]
@@ -502,7 +509,6 @@ def main() -> None:
                      "traffic": KUPDATE_TRAFFIC_BYTES if args.sim_steps % 10 == 0 else None,
                      "traffic_unit": "bytes per launch (ncu, cold L2)",
                      "algorithmic_bytes_per_launch": upd_bytes / max(1, launches),
-                     "update_ms_share": tot_upd / tot_dev if tot_dev else None,
                      "avg_update_launch_us": 1e6 * tot_upd / max(1, launches)},
         "e2e": {"value": tot_ev_all / tot_wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 4 + 8 + 4,
                 "d2h_bytes_per_step": int(d2h)},

@@ -630,33 +630,17 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
     const int lane = threadIdx.x & 31;
     const int run_t0 = *n.run_t0;
     const int T0 = run_t0 + toff;
-    // external spikes of the block's steps (InputSpike::ProcessEvent): one
-    // warp per spike marks its out-synapses like a spike of the update (their
-    // arrivals fall after this block, so marking first is safe); the raster
-    // entries are added on the host, which holds the list
-    if (n.ext_ptr) {
-        const int e0 = n.ext_ptr[toff], e1 = n.ext_ptr[toff + B];
-        const int nwarps = (gridDim.x * blockDim.x) >> 5;
-        for (int g = j >> 5; g < e1 - e0; g += nwarps) {
-            const int x = e0 + g;
-            int b = 0;
-            while (b + 1 < B && n.ext_ptr[toff + b + 1] <= x) ++b;
-            const int src = n.ext_ids[x];
-            mark_out(n, n.out_ptr[src] + lane, n.out_ptr[src + 1], (unsigned int)(T0 + b));
-        }
-    }
+    // Programmatic dependent launch: the next block's launch may start once
+    // every CTA of this one has; its prologue up to griddepcontrol.wait reads
+    // only what no launch writes (network structure, parameters, generator
+    // inputs), overlapping this launch's tail.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     Model L;
     NeuronRegs r;
     int base = 0, end = 0, woff = 0, nw = 0, tslot = -1, g0 = 0, g1 = 0;
     if (active) {
         L = load_model(n.layers[n.pop[j]]);
-        r.v = n.v[j];
-        r.u = n.u[j];
-        r.gexc = n.gexc[j];
-        r.ginh = n.ginh[j];
-        r.iext = n.iext[j];
-        r.last = n.last[j];
         base = n.csc_ptr[j];
         end = n.csc_ptr[j + 1];
         woff = n.woff[j];
@@ -677,6 +661,31 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
             gin[q].delay = n.gen_delay[g0 + q];
             gin[q].pos = n.gen_pos[g0 + q];
         }
+    }
+    // everything below reads or writes what the previous block's launch wrote
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // external spikes of the block's steps (InputSpike::ProcessEvent): one
+    // warp per spike marks its out-synapses like a spike of the update (their
+    // arrivals fall after this block, so marking first is safe); the raster
+    // entries are added on the host, which holds the list
+    if (n.ext_ptr) {
+        const int e0 = n.ext_ptr[toff], e1 = n.ext_ptr[toff + B];
+        const int nwarps = (gridDim.x * blockDim.x) >> 5;
+        for (int g = j >> 5; g < e1 - e0; g += nwarps) {
+            const int x = e0 + g;
+            int b = 0;
+            while (b + 1 < B && n.ext_ptr[toff + b + 1] <= x) ++b;
+            const int src = n.ext_ids[x];
+            mark_out(n, n.out_ptr[src] + lane, n.out_ptr[src + 1], (unsigned int)(T0 + b));
+        }
+    }
+    if (active) {
+        r.v = n.v[j];
+        r.u = n.u[j];
+        r.gexc = n.gexc[j];
+        r.ginh = n.ginh[j];
+        r.iext = n.iext[j];
+        r.last = n.last[j];
     }
     // noisy RK4 neurons: per-neuron noise key (the per-step draw is made in the step loop)
     const bool noisy = S::has(NBG_MODEL_IZH_RK4) && active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f;
@@ -1139,7 +1148,16 @@ void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int slot, bo
     const int grid = (e->N + e->threads - 1) / e->threads;
     const unsigned int flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 0], e->stream, flags);
-    e->update_kernel<<<grid, e->threads, 0, e->stream>>>(nd, B, toff);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(e->threads);
+    cfg.stream = e->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, e->update_kernel, nd, B, toff); // errors surface at the call's cudaGetLastError
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 1], e->stream, flags);
 }
 
