@@ -56,7 +56,7 @@ BYTES_PER_STATIC_EVENT = 12
 BYTES_PER_POST_UPDATE = 36
 # DRAM bytes (read + write) of one k_update launch of this workload (10 steps x
 # 100k neurons) from an ncu capture of that launch with a cold L2
-KUPDATE_TRAFFIC_BYTES = 80.6e6
+KUPDATE_TRAFFIC_BYTES = 63.0e6
 # DRAM bytes (read + write) of one dense step launch (64 x 8192, delivery and
 # update) from an ncu capture with a cold L2
 DENSE_TRAFFIC_BYTES = 277.5e6
@@ -181,6 +181,18 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _launch_shape(sim, args, trial_steps: int) -> dict:
+    """The update kernel's launch shape: autotuned, or fixed by --launch
+    THREADSxSTEPS (profiling runs, where the tuning launches would come first)."""
+    from neuronbridge_gb300 import tuning
+
+    if args.launch:
+        threads, steps = (int(x) for x in args.launch.lower().split("x"))
+        sim.set_launch(threads, steps)
+        return {"choice": {"threads_per_block": threads, "block_steps": sim.block_steps, "ms": None, "fixed": True}}
+    return tuning.autotune(sim, trial_steps=trial_steps)
+
+
 def _common(args, metric, value, unit, ms_per_step, config, **extra):
     line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -201,7 +213,7 @@ def bench_lif(args) -> dict:
     # and stretch it; the only kernel of the call is k_update, so the call's
     # device time over its launches is the launch duration
     sim = nb.Simulation(net, cfg)
-    tune = tuning.autotune(sim, trial_steps=1000)  # launch shape only; resets the simulation
+    tune = _launch_shape(sim, args, 1000)  # launch shape only; resets the simulation
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         sim.run(cfg.steps)
@@ -246,7 +258,7 @@ def bench_batched(args) -> dict:
     singles, union, cfg = workloads.batched_lif()
     build_s = time.perf_counter() - t0
     sim = nb.Simulation(union, cfg)
-    tune = tuning.autotune(sim, trial_steps=300)
+    tune = _launch_shape(sim, args, 300)
     for _ in range(args.warmup):
         sim.run(cfg.steps)
         sim.clear_spikes()
@@ -404,6 +416,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sim-steps", type=int, default=SIM_STEPS_PER_BENCH_STEP)
     ap.add_argument("--workload", default="izh", choices=["izh", "lif", "batched", "dense", "adjoint"])
+    ap.add_argument("--launch", default=None, help="fixed update-kernel launch shape THREADSxSTEPS (no autotune)")
     ap.add_argument("--per", type=int, default=None, help="simulation steps per benchmark step (dense)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -436,7 +449,7 @@ def main() -> None:
     # device time (CUDA events on the engine stream) over its launch count is
     # the average launch duration
     sim = nb.Simulation(desc, cfg, device=local, seed=2)
-    tune = tuning.autotune(sim, trial_steps=500)  # launch shape only; resets the simulation
+    tune = _launch_shape(sim, args, 500)  # launch shape only; resets the simulation
     fan = _post_fanout(desc)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
