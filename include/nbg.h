@@ -154,6 +154,13 @@ nbg_status nbg_destroy(nbg_engine *e);
  * later calls perform `steps` updates, matching the reference's run(). */
 nbg_status nbg_run(nbg_engine *e, int steps);
 nbg_status nbg_reset(nbg_engine *e);
+/* Put neurons [first, first + count) back to their initial state and drop
+ * the arrivals pending for them; synapses keep their weights and traces and
+ * the simulation time goes on.  Replaces the reset of one dense subnetwork
+ * (DenseSubnetworkModel::Reset, src/native/gpu/src/simulation_dense/
+ * DenseSubnetworkModel.cpp:173-183, reached from Simulation.reset_dense_subnetwork,
+ * python/bindings/neuronbridge_core.cpp:627-632). */
+nbg_status nbg_reset_neurons(nbg_engine *e, int first, int count);
 nbg_status nbg_next_time(const nbg_engine *e, int *t);
 nbg_status nbg_num_neurons(const nbg_engine *e, int *n);
 nbg_status nbg_num_synapses(const nbg_engine *e, int64_t *s);

@@ -83,6 +83,7 @@ _SIGNATURES = {
     "nbg_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "nbg_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nbg_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "nbg_reset_neurons": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "nbg_next_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "nbg_num_neurons": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "nbg_num_synapses": (ctypes.c_int, [ctypes.c_void_p, _i64p]),

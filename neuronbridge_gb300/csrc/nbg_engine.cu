@@ -894,6 +894,7 @@ struct nbg_engine {
     std::vector<int64_t> orig_pos; // original connection index -> CSC position
     std::vector<nbg_stdp_desc> rules;
     std::vector<float> init_v, init_u, init_iext;
+    std::vector<int> woff_host; // first mask word of each neuron (N + 1 entries)
     std::vector<float> init_w;
     // device buffers
     DevBuf<unsigned short> pop;
@@ -1369,6 +1370,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     std::vector<int> woff((size_t)e->N + 1, 0);
     for (int j = 0; j < e->N; ++j) woff[j + 1] = woff[j] + (cptr[j + 1] - cptr[j] + 31) / 32;
     e->Wt = std::max(woff[e->N], 1);
+    e->woff_host = woff;
     // ring slots: every delay plus the longest block, so that no mark made
     // inside a block aliases a slot the block drains
     e->D = e->dmax + std::min(e->dmin, kMaxBlockSteps);
@@ -1562,6 +1564,30 @@ nbg_status nbg_reset(nbg_engine *e) {
     NBG_CUDA(cudaSetDevice(e->device));
     NBG_CUDA(cudaStreamSynchronize(e->stream));
     return reset_state(e);
+}
+
+nbg_status nbg_reset_neurons(nbg_engine *e, int first, int count) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (first < 0 || count < 0 || (int64_t)first + count > e->N)
+        return fail(NBG_ERR_INVALID, "neuron range [%d, %d) outside [0, %d)", first, first + count, e->N);
+    if (count == 0) return NBG_OK;
+    NBG_CUDA(cudaSetDevice(e->device));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    const size_t f = (size_t)first, c = (size_t)count;
+    NBG_CUDA(cudaMemcpy(e->v.p + f, e->init_v.data() + f, c * sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(cudaMemcpy(e->u.p + f, e->init_u.data() + f, c * sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(cudaMemcpy(e->iext.p + f, e->init_iext.data() + f, c * sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(cudaMemset(e->gexc.p + f, 0, c * sizeof(float)));
+    NBG_CUDA(cudaMemset(e->ginh.p + f, 0, c * sizeof(float)));
+    const std::vector<int> last0(c, 10000);
+    NBG_CUDA(cudaMemcpy(e->last.p + f, last0.data(), c * sizeof(int), cudaMemcpyHostToDevice));
+    // pending arrivals: the range's mask words in every ring slot (summary
+    // bits left set only make the next drain read a zero word)
+    const int w0 = e->woff_host[f], w1 = e->woff_host[f + c];
+    if (w1 > w0)
+        NBG_CUDA(cudaMemset2D(e->mask.p + w0, (size_t)e->Wt * sizeof(unsigned int), 0,
+                              (size_t)(w1 - w0) * sizeof(unsigned int), (size_t)e->D));
+    return NBG_OK;
 }
 
 nbg_status nbg_run(nbg_engine *e, int steps) {

@@ -313,6 +313,36 @@ class SimulationConfig:
                 "event_queue": self.event_queue, "timing_wheel_size": self.timing_wheel_size}
 
 
+# models the reference's dense GPU runtime implements among this engine's
+# (NeuronModelCatalog.cpp: the DenseGpu bindings)
+DENSE_MODELS = (_lib.MODEL_LIF_VJ, _lib.MODEL_IZH_COND, _lib.MODEL_POISSON)
+
+
+def dense_name_of(layer: "NeuronLayer") -> str | None:
+    """The layer's dense subnetwork (its ``dense_subnetwork_name`` parameter),
+    validated as the reference's dense build does
+    (src/native/gpu/src/simulation_dense/DenseBuildShared.cpp:169-197, 649-653):
+    input models stay in the main network, a dense layer is not an output
+    layer, and its model must have a dense GPU implementation."""
+    name = layer.parameters.get("dense_subnetwork_name")
+    if name is None:
+        return None
+    name = str(_plain(name))
+    if not name:
+        return None
+    mid = resolve_model(layer.model)
+    if mid in (_lib.MODEL_INPUT_SPIKE, _lib.MODEL_INPUT_CURRENT):
+        raise RuntimeError(f"Input neuron model '{layer.model}' cannot be placed inside dense subnetwork "
+                           f"'{name}'; declare it in the main network and connect it to dense target neurons "
+                           "instead.")
+    if mid not in DENSE_MODELS:
+        raise RuntimeError(f"Neuron model '{layer.model}' is not supported by dense GPU subnetwork '{name}'.")
+    if layer.output:
+        raise RuntimeError("dense subnetwork layer cannot be marked isOutput=true; declare dense outputs by "
+                           "adding dense->main or dense->dense connections")
+    return name
+
+
 class NetworkDescription:
     """Flat, C-ABI-ready description (the counterpart of ``_core.NetworkDescription``)."""
 
@@ -324,6 +354,7 @@ class NetworkDescription:
         self.layer_iparams = np.zeros((n, _lib.NIP), np.int32)
         self.layer_output = np.zeros(n, bool)
         self.layer_monitored = np.zeros(n, bool)
+        self.layer_dense: list[str | None] = []  # dense_subnetwork_name of each layer (None: main network)
         for i, layer in enumerate(layers):
             mid, f, ip = layer.native_params()
             self.layer_model[i] = mid
@@ -332,6 +363,7 @@ class NetworkDescription:
             self.layer_iparams[i] = ip
             self.layer_output[i] = layer.output
             self.layer_monitored[i] = layer.monitored
+            self.layer_dense.append(dense_name_of(layer))
         parts = [c.normalized() for c in connections]
         cat = lambda key, dt: (np.concatenate([p[key] for p in parts]).astype(dt, copy=False)
                                if parts else np.zeros(0, dt))

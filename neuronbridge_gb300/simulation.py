@@ -19,9 +19,36 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib
-from .model import Network, NetworkDescription, SimulationConfig
+from .model import CATALOG, Network, NetworkDescription, SimulationConfig
 
 _SEMANTICS = {"legacy_cpu": _lib.SEM_LEGACY_CPU, "dense": _lib.SEM_DENSE}
+_MODEL_NAMES = {mid: name for name, (mid, _) in CATALOG.items()}
+
+
+def _dense_groups(desc: NetworkDescription) -> list[tuple[str, list[int]]]:
+    """(name, layer indices) of each dense subnetwork, in order of first appearance."""
+    groups: dict[str, list[int]] = {}
+    for layer, name in enumerate(getattr(desc, "layer_dense", [])):
+        if name:
+            groups.setdefault(name, []).append(layer)
+    return list(groups.items())
+
+
+def _auto_semantics(desc: NetworkDescription) -> str:
+    """Dense-runtime semantics when every layer with dynamics is in a dense
+    subnetwork, the legacy CPU semantics when none is.  Input layers always
+    belong to the main network (the reference rejects them in a subnetwork)."""
+    names = getattr(desc, "layer_dense", [None] * len(desc.layer_count))
+    dynamic = [i for i, m in enumerate(desc.layer_model)
+               if m not in (_lib.MODEL_INPUT_SPIKE, _lib.MODEL_INPUT_CURRENT)]
+    tagged = [i for i in dynamic if names[i]]
+    if not tagged:
+        return "legacy_cpu"
+    if len(tagged) == len(dynamic):
+        return "dense"
+    raise ValueError("main-network layers beside dense-subnetwork layers need the reference's interface routing, "
+                     "which the GB300 engine does not build: tag every layer with dynamics or none, or pass "
+                     "semantics='legacy_cpu' or 'dense' to run the whole network with one semantics")
 
 
 def _p(a, ct):
@@ -70,13 +97,13 @@ class Simulation:
     """High-level facade over one GB300 engine instance."""
 
     def __init__(self, network: Network | NetworkDescription | str | os.PathLike, config: SimulationConfig, *,
-                 build_options=None, device: int = 0, semantics: str = "legacy_cpu", seed: int = 0,
+                 build_options=None, device: int = 0, semantics: str = "auto", seed: int = 0,
                  block_steps: int = 0, use_graph: bool = True, threads_per_block: int = 256,
                  spike_capacity: int = 0, event_log_capacity: int = 0, kernel_timing: bool = False):
         if not isinstance(config, SimulationConfig):
             raise TypeError("Simulation expects a neuronbridge_gb300.SimulationConfig")
-        if semantics not in _SEMANTICS:
-            raise ValueError(f"semantics must be one of {sorted(_SEMANTICS)}")
+        if semantics != "auto" and semantics not in _SEMANTICS:
+            raise ValueError(f"semantics must be 'auto' or one of {sorted(_SEMANTICS)}")
         build_started = time.perf_counter()
         self.config = config
         self.lib = _lib.load()
@@ -98,6 +125,11 @@ class Simulation:
             self._build_stats = {"mode": "in_memory", "neuron_count": native.neuron_count,
                                  "connection_count": int(len(native.source))}
         self.description = native
+        self._dense_groups = _dense_groups(native)
+        if semantics == "auto":
+            semantics = _auto_semantics(native)
+        self.semantics = semantics
+        self._full_firing_export = [False] * len(self._dense_groups)
         self.flat = native.flat(config.timestep, _SEMANTICS[semantics], seed)
         desc, keep = make_desc(self.flat)
         opt = _lib.Options()
@@ -283,6 +315,102 @@ class Simulation:
     def neuron_states(self, original_neuron_ids) -> list[dict]:
         tab = self._state_table()
         return [self._state_dict(tab, int(i)) for i in original_neuron_ids]
+
+    # ------------------------------------------------------ dense subnetworks
+    # Layers tagged with a ``dense_subnetwork_name`` form the reference's dense
+    # subnetworks (one per name, numbered in order of first appearance,
+    # DenseBuildShared.cpp:655-671).  This engine runs them in its one step
+    # loop with the dense runtime's semantics; these calls mirror the
+    # reference's accessors (python/src/neuronbridge/__init__.py:179-181,
+    # 440-469; python/bindings/neuronbridge_core.cpp:574-637).
+    @property
+    def dense_subnetwork_count(self) -> int:
+        return len(self._dense_groups)
+
+    def _dense_index(self, index) -> int:
+        if isinstance(index, str):
+            found = self.find_dense_subnetwork(index)
+            if found < 0:
+                raise KeyError(f"dense subnetwork was not found: {index}")
+            return found
+        index = int(index)
+        if not 0 <= index < len(self._dense_groups):
+            raise IndexError("dense subnetwork index is out of range")
+        return index
+
+    def dense_subnetwork_name(self, index: int) -> str:
+        return self._dense_groups[self._dense_index(int(index))][0]
+
+    def find_dense_subnetwork(self, name: str) -> int:
+        for k, (n, _) in enumerate(self._dense_groups):
+            if n == name:
+                return k
+        return -1
+
+    def _dense_neurons(self, k: int) -> np.ndarray:
+        start = np.concatenate([[0], np.cumsum(self.description.layer_count)])
+        return np.concatenate([np.arange(start[l], start[l + 1]) for l in self._dense_groups[k][1]])
+
+    def _dense_synapses(self, k: int) -> np.ndarray:
+        inside = np.zeros(self.description.neuron_count, bool)
+        inside[self._dense_neurons(k)] = True
+        d = self.description
+        return np.flatnonzero(inside[d.source] & inside[d.target])
+
+    def dense_subnetwork_weights(self, index: int) -> list[float]:
+        """Weights of the subnetwork's internal synapses (both ends inside it),
+        in original connection order."""
+        k = self._dense_index(int(index))
+        return self.weights()["weight"][self._dense_synapses(k)].astype(float).tolist()
+
+    def dense_subnetwork_snapshot(self, index) -> dict:
+        """Host copy of one dense subnetwork's state (the reference's
+        DenseSubnetworkDebugSnapshot as a dict).  Arrivals live in the
+        engine's delay ring as bits, not in pending channels, so
+        ``pending_channels`` is empty."""
+        k = self._dense_index(index)
+        ids = self._dense_neurons(k)
+        tab = self._state_table()
+        fired = (tab[_lib.FIELD_LAST_SPIKE][ids] == 0) & (self.next_time > 0)
+        local_fired = np.flatnonzero(fired)
+        d = self.description
+        inside = np.zeros(d.neuron_count, bool)
+        inside[ids] = True
+        leaves = np.zeros(d.neuron_count, bool)
+        leaves[d.source[inside[d.source] & ~inside[d.target]]] = True
+        models = []
+        for m, layer in enumerate(self._dense_groups[k][1]):
+            sel = np.flatnonzero(self._layer_of[ids] == layer)
+            models.append({"factory_model_id": int(d.layer_model[layer]), "model_id": m,
+                           "legacy_model_name": _MODEL_NAMES.get(int(d.layer_model[layer]), ""),
+                           "float_state_vectors": [tab[_lib.FIELD_V][ids[sel]].astype(float).tolist(),
+                                                   tab[_lib.FIELD_U][ids[sel]].astype(float).tolist()],
+                           "byte_state_vectors": []})
+        return {"name": self._dense_groups[k][0], "time_step": max(self.next_time - 1, 0),
+                "cuda_build_enabled": True, "gpu_backend_ready": True, "carlsim_like_gpu_active": False,
+                "visible_output_firing_ids": [int(x) for x in local_fired if leaves[ids[x]]],
+                "full_firing_ids": local_fired.tolist() if self._full_firing_export[k] else [],
+                "membrane_v": tab[_lib.FIELD_V][ids].astype(float).tolist(),
+                "gexc": tab[_lib.FIELD_G_EXC][ids].astype(float).tolist(),
+                "ginh": tab[_lib.FIELD_G_INH][ids].astype(float).tolist(),
+                "fired": fired.astype(int).tolist(), "pending_channels": [],
+                "synaptic_weights": self.dense_subnetwork_weights(k), "synaptic_learning_pending_dwt": [],
+                "model_debug_states": models, "emitted_output_spikes": [], "firing_history_ring_size": 0,
+                "local_to_original_neuron_ids": ids.astype(int).tolist()}
+
+    def reset_dense_subnetwork(self, index) -> "Simulation":
+        """Initial state for the subnetwork's neurons and no pending arrivals
+        for them; weights, traces and time are kept."""
+        k = self._dense_index(index)
+        start = np.concatenate([[0], np.cumsum(self.description.layer_count)])
+        for layer in self._dense_groups[k][1]:
+            _lib.check(self.lib.nbg_reset_neurons(self._h, int(start[layer]),
+                                                   int(self.description.layer_count[layer])))
+        return self
+
+    def set_dense_subnetwork_full_firing_export_enabled(self, index, enabled: bool = True) -> "Simulation":
+        self._full_firing_export[self._dense_index(index)] = bool(enabled)
+        return self
 
     # ----------------------------------------------------------------- spikes
     def spike_raster(self) -> tuple[np.ndarray, np.ndarray]:

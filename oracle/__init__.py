@@ -88,6 +88,7 @@ def _lib(prec: int):
             "add_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             "add_external_spike": (None, [vp, ctypes.c_int, ctypes.c_int]),
             "set_decay_table": (None, [vp, ctypes.c_int64, f32p]),
+            "reset_neurons": (None, [vp, ctypes.c_int, ctypes.c_int]),
             "add_external_current": (None, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
             "dense_create": (vp, [ctypes.c_int, ctypes.c_int, f32p, f32p, i32p, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float]),
@@ -225,6 +226,10 @@ class OracleNet:
         """InputCurrent events sent over the neurons' current synapses."""
         for t, i, v in zip(np.atleast_1d(times), np.atleast_1d(neurons), np.atleast_1d(values)):
             self._f("add_external_current")(self.h, int(t), int(i), float(np.float32(v)))
+        return self
+
+    def reset_neurons(self, first: int, count: int) -> "OracleNet":
+        self._f("reset_neurons")(self.h, int(first), int(count))
         return self
 
     def set_event_log(self, on: bool = True) -> None:

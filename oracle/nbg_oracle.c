@@ -218,6 +218,33 @@ static int cmp_csc(const void *a, const void *b) {
 
 void ORC(destroy)(void *hp);
 
+/* Initial state of neuron i of layer L. */
+static void init_neuron(net_t *n, const layer_t *L, int i) {
+    n->last[i] = 10000;
+    switch (L->model) {
+    case M_LIF_VJ:
+        /* legacy: V = V_reset + random_mu (TimeDrivenLIF_Voltage_jump.cpp:37);
+         * dense profile: v = v_rest (gpu DenseLifVoltageJumpModel.h ResetStateFields) */
+        n->v[i] = n->semantics == SEM_DENSE ? L->f[0] : L->f[4] + L->f[5];
+        n->i_ext[i] = L->f[6];
+        break;
+    case M_IZH_COND:
+        /* v = V_rest, u = b*V_rest (TimeDrivenIzhikevic_Exponential_Decay.cpp:50) */
+        n->v[i] = L->f[4];
+        n->u[i] = L->f[1] * L->f[4];
+        n->i_ext[i] = L->f[11];
+        break;
+    case M_IZH_RK4:
+        n->v[i] = L->f[4];
+        n->u[i] = L->f[1] * L->f[4];
+        n->i_ext[i] = L->f[7];
+        break;
+    case M_POISSON:
+        n->i_ext[i] = L->f[2];
+        break;
+    }
+}
+
 void *ORC(create)(int n_layers, const int *model, const int *count, const float *fparams, const int *iparams,
                   int64_t n_conn, const int *src, const int *tgt, const int *type, const float *w,
                   const float *wmax, const int *delay, const int *rule, int n_rules, const float *rparams,
@@ -343,31 +370,7 @@ void *ORC(create)(int n_layers, const int *model, const int *count, const float 
     n->threads = 1;
     for (int l = 0; l < n_layers; ++l) {
         layer_t *L = &n->layers[l];
-        for (int i = L->start; i < L->start + L->count; ++i) {
-            n->last[i] = 10000;
-            switch (L->model) {
-            case M_LIF_VJ:
-                /* legacy: V = V_reset + random_mu (TimeDrivenLIF_Voltage_jump.cpp:37);
-                 * dense profile: v = v_rest (gpu DenseLifVoltageJumpModel.h ResetStateFields) */
-                n->v[i] = semantics == SEM_DENSE ? L->f[0] : L->f[4] + L->f[5];
-                n->i_ext[i] = L->f[6];
-                break;
-            case M_IZH_COND:
-                /* v = V_rest, u = b*V_rest (TimeDrivenIzhikevic_Exponential_Decay.cpp:50) */
-                n->v[i] = L->f[4];
-                n->u[i] = L->f[1] * L->f[4];
-                n->i_ext[i] = L->f[11];
-                break;
-            case M_IZH_RK4:
-                n->v[i] = L->f[4];
-                n->u[i] = L->f[1] * L->f[4];
-                n->i_ext[i] = L->f[7];
-                break;
-            case M_POISSON:
-                n->i_ext[i] = L->f[2];
-                break;
-            }
-        }
+        for (int i = L->start; i < L->start + L->count; ++i) init_neuron(n, L, i);
         if (L->model == M_IZH_COND) {
             /* conductance decay factors: host std::exp(-dt * (1/tau)) in float
              * (TimeDrivenIzhikevic_Exponential_Decay.cpp:32-39) */
@@ -893,6 +896,29 @@ void ORC(get_events)(void *hp, int *t, int64_t *conn, double *w) {
         t[k] = (int)n->ev_t.v[k];
         conn[k] = n->csc_orig[n->ev_pos.v[k]];
         w[k] = (double)n->ev_w[k];
+    }
+}
+
+/* Neurons [first, first + count) back to their initial state, with the
+ * arrivals pending for them dropped; synapses and time are kept (the reset
+ * of one dense subnetwork: DenseSubnetworkModel::Reset,
+ * src/native/gpu/src/simulation_dense/DenseSubnetworkModel.cpp:173-183). */
+void ORC(reset_neurons)(void *hp, int first, int count) {
+    net_t *n = (net_t *)hp;
+    for (int i = first; i < first + count; ++i) {
+        n->g_ampa[i] = n->g_gaba[i] = n->rate[i] = n->pend_e[i] = n->pend_i[i] = 0;
+        n->u[i] = 0;
+        n->fired[i] = 0;
+        init_neuron(n, &n->layers[n->layer_of[i]], i);
+    }
+    for (int r = 0; r < n->ring; ++r) {
+        vec64_t *b = &n->bucket[r];
+        int64_t k = 0;
+        for (int64_t q = 0; q < b->n; ++q) {
+            const int j = n->csc_tgt[b->v[q]];
+            if (j < first || j >= first + count) b->v[k++] = b->v[q];
+        }
+        b->n = k;
     }
 }
 
