@@ -79,7 +79,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
             if lg:
                 print(lg, file=sys.stderr)
     if force or _stale(LIB, objs):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart"]
+        cmd = [cc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")

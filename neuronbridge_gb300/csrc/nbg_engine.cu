@@ -43,6 +43,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
+#include <mutex>
+#include <thread>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -1054,7 +1057,21 @@ nbg_status ensure_decay_table(nbg_engine *e, int64_t needed) {
     if (e->n_rules == 0) return NBG_OK;
     if (e->dtab_complete || e->dtab_len >= needed) return NBG_OK;
     if (e->semantics == NBG_SEM_DENSE) return dense_decay_table(e);
-    int64_t len = std::max<int64_t>(needed, 4096);
+    // Entry k does not depend on the table's length, so the table is grown
+    // ahead of need: at least doubled, and at once to the length where every
+    // row has underflowed to 0 when that is at most 2^22 entries.  It (and the
+    // CUDA graph holding its address) is then rebuilt a few times per
+    // simulation instead of at every run call.
+    int64_t full = 1;
+    for (int r = 0; r < e->n_rules; ++r)
+        for (const float tau : {e->rules[r].ltp_tau, e->rules[r].ltd_tau}) {
+            const float inv = (float)(1.0 / (double)tau);
+            int64_t k = 1;
+            while ((float)k * e->dt * inv <= 104.0f && k < ((int64_t)1 << 24)) k *= 2;
+            full = std::max(full, k + 1);
+        }
+    int64_t len = std::max<int64_t>({needed, (int64_t)4096, 2 * (int64_t)e->dtab_len});
+    if (full <= ((int64_t)1 << 22)) len = std::max(len, full);
     len = std::min<int64_t>(len, (int64_t)1 << 24);
     std::vector<float> tab((size_t)e->n_rules * 2 * len);
     bool complete = true;
@@ -1172,6 +1189,92 @@ nbg_status harvest_timing(nbg_engine *e, int blocks) {
         e->last_upd_ms += a;
     }
     return NBG_OK;
+}
+
+// Reusable barrier for the raster assembly threads.
+class Barrier {
+  public:
+    explicit Barrier(int n) : n_(n) {}
+    void wait() {
+        std::unique_lock<std::mutex> lk(m_);
+        const unsigned long long gen = gen_;
+        if (++arrived_ == n_) {
+            arrived_ = 0;
+            ++gen_;
+            cv_.notify_all();
+        } else {
+            cv_.wait(lk, [&] { return gen_ != gen; });
+        }
+    }
+
+  private:
+    std::mutex m_;
+    std::condition_variable cv_;
+    int n_, arrived_ = 0;
+    unsigned long long gen_ = 0;
+};
+
+// Append one run call's raster to spk_t / spk_id in (step, id) order.  The
+// device entries (ts, ids) come in warp order; ext holds the external spikes
+// of recorded neurons, which follow the device entries of their step before
+// the ids of each step are sorted.  A counting sort by step (per-thread
+// histograms over contiguous chunks, one prefix pass, a scatter) and the
+// per-step sorts run on up to 16 host threads for large rasters.
+void assemble_raster(nbg_engine *e, const std::vector<int> &ts, const std::vector<int> &ids,
+                     const std::vector<std::pair<int, int>> &ext, int t0, int count) {
+    const size_t n = ids.size(), steps = (size_t)count;
+    const size_t total = n + ext.size();
+    const size_t base = e->spk_id.size();
+    e->spk_id.resize(base + total);
+    e->spk_t.resize(base + total);
+    int *out_id = e->spk_id.data() + base, *out_t = e->spk_t.data() + base;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = n >= ((size_t)1 << 16) ? (int)std::min(16u, hw) : 1;
+    std::vector<size_t> hist((size_t)T * steps, 0); // thread k, step s: count, then write position
+    std::vector<size_t> at(steps + 1, 0);           // first position of each step
+    auto chunk_begin = [&](int k) { return n * (size_t)k / (size_t)T; };
+    auto body = [&](int k, Barrier *bar) {
+        size_t *h = hist.data() + (size_t)k * steps;
+        for (size_t i = chunk_begin(k); i < chunk_begin(k + 1); ++i) ++h[(size_t)(ts[i] - t0)];
+        if (bar) bar->wait();
+        if (k == 0) { // write positions: step by step, thread chunks in order, then external spikes
+            std::vector<size_t> ext_cnt(steps, 0), next_ext(steps, 0);
+            for (const auto &x : ext) ++ext_cnt[(size_t)(x.first - t0)];
+            size_t pos = 0;
+            for (size_t st = 0; st < steps; ++st) {
+                at[st] = pos;
+                for (int q = 0; q < T; ++q) {
+                    size_t &hq = hist[(size_t)q * steps + st];
+                    const size_t c = hq;
+                    hq = pos;
+                    pos += c;
+                }
+                next_ext[st] = pos;
+                pos += ext_cnt[st];
+            }
+            at[steps] = pos;
+            for (const auto &x : ext) out_id[next_ext[(size_t)(x.first - t0)]++] = x.second;
+        }
+        if (bar) bar->wait();
+        for (size_t i = chunk_begin(k); i < chunk_begin(k + 1); ++i) out_id[h[(size_t)(ts[i] - t0)]++] = ids[i];
+        if (bar) bar->wait();
+        // steps whose first entry falls in this thread's share of the output
+        const size_t lo = total * (size_t)k / (size_t)T, hi = total * (size_t)(k + 1) / (size_t)T;
+        size_t st = (size_t)(std::lower_bound(at.begin(), at.end() - 1, lo) - at.begin());
+        for (; st < steps && at[st] < hi; ++st) {
+            std::sort(out_id + at[st], out_id + at[st + 1]);
+            std::fill(out_t + at[st], out_t + at[st + 1], t0 + (int)st);
+        }
+    };
+    if (T == 1) {
+        body(0, nullptr);
+        return;
+    }
+    Barrier bar(T);
+    std::vector<std::thread> pool;
+    for (int k = 1; k < T; ++k) pool.emplace_back(body, k, &bar);
+    body(0, &bar);
+    for (auto &th : pool) th.join();
 }
 
 } // namespace
@@ -1778,23 +1881,11 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         NBG_CUDA(cudaMemcpy(ids.data(), e->out_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
         NBG_CUDA(cudaMemcpy(ts.data(), e->out_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
     }
-    std::vector<size_t> at((size_t)count + 1, 0);
-    for (size_t k = 0; k < (size_t)ndev; ++k) at[(size_t)(ts[k] - t0) + 1]++;
-    for (const auto &x : ext_due)
-        if (e->layers[e->pop_host[x.second]].record) at[(size_t)(x.first - t0) + 1]++;
-    for (int k = 0; k < count; ++k) at[(size_t)k + 1] += at[(size_t)k];
-    const size_t base = e->spk_id.size();
-    e->spk_id.resize(base + at[(size_t)count]);
-    e->spk_t.resize(base + at[(size_t)count]);
     {
-        std::vector<size_t> fill(at.begin(), at.end() - 1);
-        for (size_t k = 0; k < (size_t)ndev; ++k) e->spk_id[base + fill[(size_t)(ts[k] - t0)]++] = ids[k];
+        std::vector<std::pair<int, int>> ext_rec; // external spikes of recorded neurons
         for (const auto &x : ext_due)
-            if (e->layers[e->pop_host[x.second]].record) e->spk_id[base + fill[(size_t)(x.first - t0)]++] = x.second;
-    }
-    for (int k = 0; k < count; ++k) {
-        std::sort(e->spk_id.begin() + base + at[(size_t)k], e->spk_id.begin() + base + at[(size_t)k + 1]);
-        std::fill(e->spk_t.begin() + base + at[(size_t)k], e->spk_t.begin() + base + at[(size_t)k + 1], t0 + k);
+            if (e->layers[e->pop_host[x.second]].record) ext_rec.push_back(x);
+        assemble_raster(e, ts, ids, ext_rec, t0, count);
     }
     if (ntr > 0) {
         const size_t rb = e->trace_rows.size();

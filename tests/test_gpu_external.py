@@ -159,3 +159,31 @@ def test_external_input_errors():
     bad.connect(Connection(0, 2, synapse_type=0, weight=1.0, delay=1))
     with pytest.raises(nb.NbgError, match="current synapses"):
         nb.Simulation(bad, cfg)
+
+
+def test_large_raster_with_external_spikes_bit_exact(oracle_lib):
+    """Above 65,536 raster entries per run call the host assembles the raster
+    on several threads; external spikes of recorded input neurons interleave
+    with the device entries of their steps."""
+    n_poi, n_in = 3000, 64
+    net = Network()
+    net.add_layer(NeuronLayer.input_spike(n_in, output=True))
+    net.add_layer(NeuronLayer("PoissonRate", n_poi, output=True,
+                              parameters={"poisson_rate_bias_hz": float32(400.0),
+                                          "poisson_rate_gain_hz_per_current": float32(0.0)}))
+    net.add_layer(NeuronLayer("TimeDrivenLIF_Voltage_jump", 100, output=True))
+    rng = np.random.default_rng(4)
+    src = rng.integers(0, n_in + n_poi, 5000).astype(np.int32)
+    tgt = rng.integers(n_in + n_poi, n_in + n_poi + 100, 5000).astype(np.int32)
+    net.connect(Connection(src, tgt, synapse_type=0, weight=0.3, delay=rng.integers(1, 9, 5000).astype(np.int32)))
+    cfg = SimulationConfig(steps=700, timestep=0.1)
+    sim = nb.Simulation(net, cfg)
+    o = _oracle(net, cfg)
+    pick = rng.choice(700 * n_in, 900, replace=False)
+    t, i = pick // n_in, pick % n_in
+    sim.add_external_spikes(t, i)
+    o.add_external_spikes(t, i)
+    sim.run()
+    o.run(cfg.steps)
+    assert len(sim.spike_raster()[0]) > 65536
+    _same(sim, o, net)
