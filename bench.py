@@ -257,7 +257,7 @@ def bench_batched(args) -> dict:
     t0 = time.perf_counter()
     singles, union, cfg = workloads.batched_lif()
     build_s = time.perf_counter() - t0
-    sim = nb.Simulation(union, cfg)
+    sim = nb.Simulation.batch(singles, cfg)  # one engine over the 256 instances (nbg_create_batch)
     tune = _launch_shape(sim, args, 300)
     for _ in range(args.warmup):
         sim.run(cfg.steps)

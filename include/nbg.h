@@ -150,6 +150,20 @@ void nbg_default_options(nbg_options *opt);
 nbg_status nbg_create(const nbg_net_desc *desc, const nbg_options *opt, nbg_engine **out);
 nbg_status nbg_destroy(nbg_engine *e);
 
+/* One engine over n independent networks (the batched form of nbg_create:
+ * one step loop and one launch per block for all of them).  Layers,
+ * connections and learning rules are concatenated, instance k's neuron ids
+ * offset by the neurons of instances 0..k-1 and its rule ids by their rules;
+ * ids are checked per instance.  first_neuron (n + 1 entries, may be null)
+ * receives each instance's first engine neuron id and the total.  All
+ * instances share dt_ms, semantics and seed; PoissonRate draws are local to
+ * their layer, so every instance behaves exactly as when created alone,
+ * except the noise of IZH_RK4 layers, which is keyed by the engine-wide
+ * neuron id.  The reference creates one Simulation per network
+ * (src/native/legacy/source_file_realtime_v1_async/Simulation/inc/Simulation.h:187-250). */
+nbg_status nbg_create_batch(const nbg_net_desc *const *descs, int n, const nbg_options *opt, nbg_engine **out,
+                            int64_t *first_neuron);
+
 /* Advance the network.  The first call performs steps+1 updates (t=0..steps),
  * later calls perform `steps` updates, matching the reference's run(). */
 nbg_status nbg_run(nbg_engine *e, int steps);

@@ -80,6 +80,8 @@ _SIGNATURES = {
     "nbg_version": (ctypes.c_char_p, []),
     "nbg_default_options": (None, [ctypes.POINTER(Options)]),
     "nbg_create": (ctypes.c_int, [ctypes.POINTER(NetDesc), ctypes.POINTER(Options), ctypes.POINTER(ctypes.c_void_p)]),
+    "nbg_create_batch": (ctypes.c_int, [ctypes.POINTER(ctypes.POINTER(NetDesc)), ctypes.c_int, ctypes.POINTER(Options),
+                                        ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64)]),
     "nbg_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "nbg_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nbg_reset": (ctypes.c_int, [ctypes.c_void_p]),

@@ -1296,6 +1296,79 @@ void nbg_default_options(nbg_options *o) {
     o->kernel_timing = 0;
 }
 
+nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engine **out);
+
+nbg_status nbg_create_batch(const nbg_net_desc *const *descs, int n, const nbg_options *opt, nbg_engine **out,
+                            int64_t *first_neuron) {
+    if (!descs || !out || n <= 0) return fail(NBG_ERR_INVALID, "need at least one network description");
+    *out = nullptr;
+    std::vector<nbg_layer_desc> layers;
+    std::vector<int32_t> src, tgt, type, delay, rule;
+    std::vector<float> w, wmax;
+    std::vector<nbg_stdp_desc> rules;
+    std::vector<int64_t> first((size_t)n + 1, 0);
+    int64_t off = 0;
+    int roff = 0;
+    for (int k = 0; k < n; ++k) {
+        const nbg_net_desc *d = descs[k];
+        if (!d || !d->layers || d->n_layers <= 0) return fail(NBG_ERR_INVALID, "instance %d: no layers", k);
+        if (d->dt_ms != descs[0]->dt_ms || d->semantics != descs[0]->semantics || d->seed != descs[0]->seed)
+            return fail(NBG_ERR_INVALID, "instance %d: every instance must share dt_ms, semantics and seed", k);
+        if (d->n_conn < 0 || (d->n_conn > 0 && (!d->source || !d->target || !d->type || !d->weight ||
+                                                !d->max_weight || !d->delay || !d->rule)))
+            return fail(NBG_ERR_INVALID, "instance %d: connection arrays must be non-null", k);
+        if (d->n_rules < 0 || (d->n_rules > 0 && !d->rules))
+            return fail(NBG_ERR_INVALID, "instance %d: bad learning rules", k);
+        int64_t count = 0;
+        for (int l = 0; l < d->n_layers; ++l) {
+            if (d->layers[l].count <= 0) return fail(NBG_ERR_INVALID, "instance %d layer %d: count must be positive", k, l);
+            count += d->layers[l].count;
+            layers.push_back(d->layers[l]);
+        }
+        // ids are checked per instance: an id past the instance's end would
+        // otherwise land in the next instance
+        for (int64_t c = 0; c < d->n_conn; ++c) {
+            if (d->source[c] < 0 || d->source[c] >= count || d->target[c] < 0 || d->target[c] >= count)
+                return fail(NBG_ERR_INVALID, "instance %d connection %lld: neuron id out of range", k, (long long)c);
+            if (d->rule[c] >= d->n_rules)
+                return fail(NBG_ERR_INVALID, "instance %d connection %lld: unknown learning rule", k, (long long)c);
+            src.push_back((int32_t)(d->source[c] + off));
+            tgt.push_back((int32_t)(d->target[c] + off));
+            type.push_back(d->type[c]);
+            w.push_back(d->weight[c]);
+            wmax.push_back(d->max_weight[c]);
+            delay.push_back(d->delay[c]);
+            rule.push_back(d->rule[c] < 0 ? d->rule[c] : d->rule[c] + roff);
+        }
+        for (int r = 0; r < d->n_rules; ++r) rules.push_back(d->rules[r]);
+        first[(size_t)k] = off;
+        off += count;
+        roff += d->n_rules;
+        if (off > (1 << 30)) return fail(NBG_ERR_INVALID, "too many neurons");
+    }
+    first[(size_t)n] = off;
+    if (layers.size() > 65535) return fail(NBG_ERR_INVALID, "need 1..65535 layers in all");
+    nbg_net_desc u{};
+    u.n_layers = (int)layers.size();
+    u.layers = layers.data();
+    u.n_conn = (int64_t)src.size();
+    u.source = src.data();
+    u.target = tgt.data();
+    u.type = type.data();
+    u.weight = w.data();
+    u.max_weight = wmax.data();
+    u.delay = delay.data();
+    u.rule = rule.data();
+    u.n_rules = (int)rules.size();
+    u.rules = rules.data();
+    u.dt_ms = descs[0]->dt_ms;
+    u.semantics = descs[0]->semantics;
+    u.seed = descs[0]->seed;
+    const nbg_status st = nbg_create(&u, opt, out);
+    if (st == NBG_OK && first_neuron) std::copy(first.begin(), first.end(), first_neuron);
+    return st;
+}
+
 nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engine **out) {
     if (!d || !out) return fail(NBG_ERR_INVALID, "null argument");
     *out = nullptr;

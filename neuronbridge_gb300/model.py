@@ -403,6 +403,32 @@ class NetworkDescription:
             raise ValueError("connection arrays must have one entry per connection")
         return d
 
+    @classmethod
+    def concat(cls, parts: list["NetworkDescription"]) -> tuple["NetworkDescription", np.ndarray, np.ndarray]:
+        """Independent networks as one description (the host form of
+        nbg_create_batch): layers, connections and learning rules
+        concatenated, neuron ids of part k offset by the neurons of parts
+        0..k-1 and its rule ids by their rules.  Returns (union, first
+        neuron of each part + total, first connection of each part + total)."""
+        if not parts:
+            raise ValueError("need at least one network")
+        d = cls([], [], [])
+        neurons = np.array([0] + [p.neuron_count for p in parts], np.int64).cumsum()
+        conns = np.array([0] + [len(p.source) for p in parts], np.int64).cumsum()
+        rules = np.array([0] + [len(p.rule_params) for p in parts], np.int64).cumsum()
+        for key in ("layer_model", "layer_count", "layer_fparams", "layer_iparams", "layer_output", "layer_monitored"):
+            setattr(d, key, np.concatenate([getattr(p, key) for p in parts]))
+        d.layer_dense = [name for p in parts for name in getattr(p, "layer_dense", [None] * len(p.layer_count))]
+        d.source = np.concatenate([p.source + neurons[k] for k, p in enumerate(parts)]).astype(np.int32)
+        d.target = np.concatenate([p.target + neurons[k] for k, p in enumerate(parts)]).astype(np.int32)
+        for key in ("type", "weight", "max_weight", "delay"):
+            setattr(d, key, np.concatenate([getattr(p, key) for p in parts]))
+        d.rule = np.concatenate([np.where(p.rule >= 0, p.rule + rules[k], p.rule)
+                                 for k, p in enumerate(parts)]).astype(np.int32)
+        d.rule_params = (np.concatenate([p.rule_params for p in parts]).astype(np.float32) if rules[-1]
+                         else np.zeros((0, 4), np.float32))
+        return d, neurons, conns
+
     @property
     def neuron_count(self) -> int:
         return int(self.layer_count.sum())

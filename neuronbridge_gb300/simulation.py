@@ -99,7 +99,8 @@ class Simulation:
     def __init__(self, network: Network | NetworkDescription | str | os.PathLike, config: SimulationConfig, *,
                  build_options=None, device: int = 0, semantics: str = "auto", seed: int = 0,
                  block_steps: int = 0, use_graph: bool = True, threads_per_block: int = 256,
-                 spike_capacity: int = 0, event_log_capacity: int = 0, kernel_timing: bool = False):
+                 spike_capacity: int = 0, event_log_capacity: int = 0, kernel_timing: bool = False,
+                 _instances: list | None = None):
         if not isinstance(config, SimulationConfig):
             raise TypeError("Simulation expects a neuronbridge_gb300.SimulationConfig")
         if semantics != "auto" and semantics not in _SEMANTICS:
@@ -131,7 +132,8 @@ class Simulation:
         self.semantics = semantics
         self._full_firing_export = [False] * len(self._dense_groups)
         self.flat = native.flat(config.timestep, _SEMANTICS[semantics], seed)
-        desc, keep = make_desc(self.flat)
+        if _instances is None:
+            desc, keep = make_desc(self.flat)
         opt = _lib.Options()
         self.lib.nbg_default_options(ctypes.byref(opt))
         opt.device = int(device)
@@ -142,7 +144,16 @@ class Simulation:
         opt.event_log_capacity = int(event_log_capacity)
         opt.kernel_timing = int(bool(kernel_timing))
         h = ctypes.c_void_p()
-        st = self.lib.nbg_create(ctypes.byref(desc), ctypes.byref(opt), ctypes.byref(h))
+        if _instances is None:
+            st = self.lib.nbg_create(ctypes.byref(desc), ctypes.byref(opt), ctypes.byref(h))
+        else:  # one engine over the instances (nbg_create_batch)
+            made = [make_desc(p.flat(config.timestep, _SEMANTICS[semantics], seed)) for p in _instances]
+            ptrs = (ctypes.POINTER(_lib.NetDesc) * len(made))(*[ctypes.pointer(m[0]) for m in made])
+            first = np.zeros(len(made) + 1, np.int64)
+            st = self.lib.nbg_create_batch(ptrs, len(made), ctypes.byref(opt), ctypes.byref(h),
+                                           _p(first, ctypes.c_int64))
+            if st == 0 and not np.array_equal(first, self.instance_first):
+                raise RuntimeError("nbg_create_batch placed the instances differently from the host union")
         if st == 1:
             raise ValueError(self.lib.nbg_last_error().decode())
         _lib.check(st)
@@ -159,6 +170,42 @@ class Simulation:
         self._extra_recorded = False  # layers recorded for the monitor beyond the outputs
         self._monitor = None
         self._build_stats["total_build_seconds"] = time.perf_counter() - build_started
+
+    @classmethod
+    def batch(cls, networks, config: SimulationConfig, **kwargs) -> "Simulation":
+        """One engine over independent networks: one step loop and one launch
+        per block for all of them (nbg_create_batch).  Instance k owns engine
+        neurons [instance_first[k], instance_first[k + 1]) and connections
+        [instance_conn_first[k], instance_conn_first[k + 1]); results per
+        instance equal those of the network run alone (noisy
+        IzhikevichCurrentRK4 layers excepted: their noise is keyed by the
+        engine-wide neuron id)."""
+        parts = [n.to_native() if isinstance(n, Network) else n for n in networks]
+        if not parts or not all(isinstance(p, NetworkDescription) for p in parts):
+            raise TypeError("Simulation.batch expects a non-empty list of Network or NetworkDescription")
+        union, first, conn_first = NetworkDescription.concat(parts)
+        sim = cls.__new__(cls)
+        sim.instance_first, sim.instance_conn_first = first, conn_first
+        cls.__init__(sim, union, config, _instances=parts, **kwargs)
+        return sim
+
+    @property
+    def instance_count(self) -> int:
+        first = getattr(self, "instance_first", None)
+        return 1 if first is None else len(first) - 1
+
+    def instance_raster(self, k: int) -> tuple[np.ndarray, np.ndarray]:
+        """Spikes of instance k of a batch as (times, instance-local ids)."""
+        a, b = self.instance_first[k], self.instance_first[k + 1]
+        t, i = self.spike_raster()
+        keep = (i >= a) & (i < b)
+        return t[keep], (i[keep] - a).astype(np.int32)
+
+    def instance_state(self, k: int, field: int) -> np.ndarray:
+        return self.state_field(field)[self.instance_first[k]:self.instance_first[k + 1]]
+
+    def instance_weights(self, k: int) -> np.ndarray:
+        return self.weights()["weight"][self.instance_conn_first[k]:self.instance_conn_first[k + 1]]
 
     @property
     def build_stats(self) -> dict:
