@@ -51,12 +51,16 @@ SIM_STEPS_PER_BENCH_STEP = 10_000
 #   delivered event: plastic 40 B (index 4, weight r/w 8, Apre/Apost/last r/w 24,
 #   mask bit 4), non-plastic 12 B; post-STDP: 36 B per (post spike x plastic in-synapse)
 BYTES_PER_NEURON_STEP = 32
+BYTES_PER_LIF_NEURON_STEP = 24  # V r/w 8, refractory counter r/w 8, ring word read+clear 8
 BYTES_PER_PLASTIC_EVENT = 40
 BYTES_PER_STATIC_EVENT = 12
 BYTES_PER_POST_UPDATE = 36
 # DRAM bytes (read + write) of one k_update launch of this workload (10 steps x
 # 100k neurons) from an ncu capture of that launch with a cold L2
 KUPDATE_TRAFFIC_BYTES = 63.0e6
+# DRAM bytes (read + write) of one k_update launch of the 256-instance batched
+# workload (15 steps), scaled from an ncu capture on its first 32 instances
+BATCHED_TRAFFIC_BYTES = None
 # DRAM bytes (read + write) of one dense step launch (64 x 8192, delivery and
 # update) from an ncu capture with a cold L2
 DENSE_TRAFFIC_BYTES = 277.5e6
@@ -255,7 +259,7 @@ def bench_batched(args) -> dict:
     from neuronbridge_gb300 import tuning, workloads
 
     t0 = time.perf_counter()
-    singles, union, cfg = workloads.batched_lif()
+    singles, union, cfg = workloads.batched_lif(instances=args.instances)
     build_s = time.perf_counter() - t0
     sim = nb.Simulation.batch(singles, cfg)  # one engine over the 256 instances (nbg_create_batch)
     tune = _launch_shape(sim, args, 300)
@@ -278,6 +282,7 @@ def bench_batched(args) -> dict:
         sim.clear_spikes()
     clk = clocks.stop()
     n_lif = union.neuron_count // 2
+    block_steps = sim.block_steps
     del sim
     # plain form: every instance in its own engine, one after another
     p_ev = p_dev = p_wall = 0.0
@@ -293,10 +298,23 @@ def bench_batched(args) -> dict:
         s.close()
     value = ev / dev
     plain = p_ev / p_dev
+    # the Poisson layers have no inputs: the engine evaluates them inline at
+    # their targets, so the neuron-steps are the LIF neurons'
+    upd_bytes = BYTES_PER_LIF_NEURON_STEP * n_lif * cfg.steps * args.steps + BYTES_PER_STATIC_EVENT * ev
+    peak, kind = _peaks()
+    per_launch = launches / args.steps
     return _common(args, "synaptic events/s", value, "synaptic events/s", 1e3 * dev / args.steps,
-                   {"workload": "batched_lif_256", "instances": 256, "lif_neurons": n_lif,
-                    "sim_steps_per_step": cfg.steps, "tuned": tune["choice"], "host_build_s": build_s},
+                   {"workload": f"batched_lif_{args.instances}", "instances": args.instances, "lif_neurons": n_lif,
+                    "sim_steps_per_step": cfg.steps, "block_steps": block_steps, "tuned": tune["choice"],
+                    "host_build_s": build_s},
                    neuron_steps_per_s=n_lif * cfg.steps * args.steps / dev,
+                   roofline={"bound": "hbm", "kernel": "k_update<Spec<9, 0>> (LIF + inline Poisson, static)",
+                             "achieved": upd_bytes / dev / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": upd_bytes / dev / 1e9 / peak, "peak_kind": kind,
+                             "traffic": (BATCHED_TRAFFIC_BYTES if args.instances == 256 else None),
+                             "traffic_unit": "bytes per launch (ncu on 32 instances, scaled by units)",
+                             "algorithmic_bytes_per_launch": upd_bytes / (per_launch * args.steps),
+                             "avg_update_launch_us": 1e6 * dev / launches if launches else None},
                    plain={"value": plain, "unit": "synaptic events/s", "device_s_per_1000_steps": p_dev,
                           "wall_s_per_1000_steps": p_wall},
                    speedup_vs_plain=value / plain,
@@ -416,6 +434,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sim-steps", type=int, default=SIM_STEPS_PER_BENCH_STEP)
     ap.add_argument("--workload", default="izh", choices=["izh", "lif", "batched", "dense", "adjoint"])
+    ap.add_argument("--instances", type=int, default=256, help="batched workload: number of instances")
     ap.add_argument("--launch", default=None, help="fixed update-kernel launch shape THREADSxSTEPS (no autotune)")
     ap.add_argument("--per", type=int, default=None, help="simulation steps per benchmark step (dense)")
     args = ap.parse_args()

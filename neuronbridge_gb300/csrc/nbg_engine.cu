@@ -137,6 +137,11 @@ struct NetDev {
     // external spikes of the current run call: ext_ids[ext_ptr[k] .. ext_ptr[k+1])
     // spike at call step k (null until the first nbg_add_external_spikes)
     const int *ext_ptr, *ext_ids;
+    // thread -> neuron: the first N_upd threads update upd_ids[thread] (the
+    // thread's own index when null); generator neurons gen_ids[0 .. N_gen)
+    // follow in trailing CTAs, kGenPerThread per thread
+    int N_upd, N_gen;
+    const int *upd_ids, *gen_ids;
 };
 
 __device__ __forceinline__ float hash_uniform01(int neuron_index, int time_step) {
@@ -625,11 +630,73 @@ __device__ __forceinline__ void mark_out(const NetDev &n, int q, int q1, unsigne
     }
 }
 
+// Generator neurons (PoissonRate layers without inputs: their targets draw
+// their spikes inline) need only their own spike draws, for the raster and
+// their LastSpike counter.  kGenPerThread of them per thread keeps them from
+// occupying a thread slot each.
+constexpr int kGenPerThread = 8;
+
+// The B steps of the generator neurons of thread g: PoissonRate::UpdateState
+// with no inputs (as update_neuron's POISSON case with acc = 0), raster
+// entries of recorded layers reserved once per warp.
+__device__ __forceinline__ void generator_steps(const NetDev &n, int g, int B, int T0, int run_t0, int lane) {
+    unsigned int fired[kGenPerThread];
+    int nrec = 0;
+#pragma unroll
+    for (int q = 0; q < kGenPerThread; ++q) {
+        fired[q] = 0u;
+        const int x = g * kGenPerThread + q;
+        if (x < n.N_gen) {
+            const int k = n.gen_ids[x];
+            int local;
+            const float prob = generator_prob(n, k, &local);
+            int last = n.last[k];
+            const int tslot = n.trace_slot ? n.trace_slot[k] : -1;
+            for (int b = 0; b < B; ++b) {
+                if (hash_uniform01(local, T0 + b) < prob) {
+                    last = 0;
+                    fired[q] |= 1u << b;
+                } else {
+                    last += 1;
+                }
+                if (tslot >= 0) n.trace[(size_t)(T0 + b - run_t0) * n.ntrace + tslot] = n.v[k];
+            }
+            n.last[k] = last;
+            if (n.layers[n.pop[k]].record) nrec += __popc(fired[q]);
+            else fired[q] = 0u;
+        }
+    }
+    int incl = nrec;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return;
+    unsigned int pos = 0;
+    if (lane == 31) pos = atomicAdd(n.cursor, (unsigned int)total);
+    pos = __shfl_sync(0xffffffffu, pos, 31) + (unsigned int)(incl - nrec);
+    if (nrec == 0) return;
+    if (pos + (unsigned int)nrec > (unsigned int)n.out_cap) {
+        atomicOr(n.err, kErrOverflow);
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < kGenPerThread; ++q)
+        for (unsigned int m = fired[q]; m; m &= m - 1u, ++pos) {
+            n.out_ids[pos] = n.gen_ids[g * kGenPerThread + q];
+            n.out_t[pos] = T0 + __ffs(m) - 1;
+        }
+}
+
 // One block of B steps starting toff steps after the run call's first step.
 template <class S>
 __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B, int toff) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = j < n.N;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int reg_blocks = (n.N_upd + (int)blockDim.x - 1) / (int)blockDim.x;
+    const bool gen_block = (int)blockIdx.x >= reg_blocks;
+    const bool active = !gen_block && tid < n.N_upd;
+    const int j = active && n.upd_ids ? n.upd_ids[tid] : tid;
     const int lane = threadIdx.x & 31;
     const int run_t0 = *n.run_t0;
     const int T0 = run_t0 + toff;
@@ -674,13 +741,17 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
     if (n.ext_ptr) {
         const int e0 = n.ext_ptr[toff], e1 = n.ext_ptr[toff + B];
         const int nwarps = (gridDim.x * blockDim.x) >> 5;
-        for (int g = j >> 5; g < e1 - e0; g += nwarps) {
+        for (int g = tid >> 5; g < e1 - e0; g += nwarps) {
             const int x = e0 + g;
             int b = 0;
             while (b + 1 < B && n.ext_ptr[toff + b + 1] <= x) ++b;
             const int src = n.ext_ids[x];
             mark_out(n, n.out_ptr[src] + lane, n.out_ptr[src + 1], (unsigned int)(T0 + b));
         }
+    }
+    if (gen_block) { // whole CTAs of generator threads
+        generator_steps(n, tid - reg_blocks * (int)blockDim.x, B, T0, run_t0, lane);
+        return;
     }
     if (active) {
         r.v = n.v[j];
@@ -848,7 +919,7 @@ __global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDe
     while (pbal) {
         const int l = __ffs(pbal) - 1;
         pbal &= pbal - 1u;
-        const int jl = j - lane + l;
+        const int jl = __shfl_sync(0xffffffffu, j, l);
         const unsigned int steps = __shfl_sync(0xffffffffu, spk_steps, l);
         const int q1 = n.out_ptr[jl + 1];
 #pragma unroll 2
@@ -933,6 +1004,8 @@ struct nbg_engine {
     std::unordered_set<uint64_t> ext_keys;
     std::vector<int> ext_ptr_h, ext_ids_h;
     DevBuf<int> ext_ptr_d, ext_ids_d;
+    DevBuf<int> upd_ids_d, gen_ids_d; // thread map (NetDev::upd_ids, gen_ids)
+    int N_upd = 0, N_gen = 0;
     // current synapses (type 3): per source the out-going ones (target,
     // delay, latch slot); latch slots are grouped by target in CSC order
     std::vector<int> cur_out_ptr, cur_out_tgt, cur_out_delay, cur_out_slot;
@@ -1015,6 +1088,10 @@ struct nbg_engine {
         n.n_events = n_events.p;
         n.ext_ptr = ext_ptr_d.p;
         n.ext_ids = ext_ids_d.p;
+        n.N_upd = N_upd;
+        n.N_gen = N_gen;
+        n.upd_ids = upd_ids_d.p;
+        n.gen_ids = gen_ids_d.p;
         return n;
     }
 };
@@ -1163,7 +1240,8 @@ nbg_status ensure_timing_events(nbg_engine *e, int blocks) {
 // Inside stream capture an event record must be "external" to become an
 // event-record node of the graph (a plain record is only a dependency).
 void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int slot, bool capturing = false) {
-    const int grid = (e->N + e->threads - 1) / e->threads;
+    const int gen_threads = (e->N_gen + kGenPerThread - 1) / kGenPerThread;
+    const int grid = std::max(1, (e->N_upd + e->threads - 1) / e->threads + (gen_threads + e->threads - 1) / e->threads);
     const unsigned int flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     if (e->kernel_timing) cudaEventRecordWithFlags(e->tev[2 * slot + 0], e->stream, flags);
     cudaLaunchConfig_t cfg = {};
@@ -1693,6 +1771,17 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(e->gen_pos.upload(gpos), "gen_pos");
     chk(e->gen_src.upload(gsrc), "gen_src");
     chk(e->gen_delay.upload(gdelay), "gen_delay");
+    // thread map: generator neurons leave the one-thread-per-neuron grid
+    {
+        std::vector<int> upd, gen;
+        for (int i = 0; i < e->N; ++i) (e->layers[pop[i]].generator ? gen : upd).push_back(i);
+        e->N_upd = (int)upd.size();
+        e->N_gen = (int)gen.size();
+        bool prefix = true; // updated neurons 0..N_upd-1: no map needed
+        for (int i = 0; i < e->N_upd && prefix; ++i) prefix = upd[(size_t)i] == i;
+        if (!prefix) chk(e->upd_ids_d.upload(upd), "thread map");
+        if (!gen.empty()) chk(e->gen_ids_d.upload(gen), "generator ids");
+    }
     chk(e->err.alloc(1), "err");
     chk(e->run_t0.alloc(1), "run_t0");
     chk(e->cursor.alloc(1), "cursor");
