@@ -237,6 +237,10 @@ __device__ __forceinline__ Model load_model(const LayerDev &L) {
 template <unsigned kModels, int kPlastic>
 struct Spec {
     static constexpr bool has(int m) { return (kModels >> m) & 1u; }
+    // resident 256-thread CTAs per SM the register budget is sized for: the
+    // static instances fit in 64 registers, which matters when a large
+    // network runs in several waves
+    static constexpr int min_blocks = kPlastic == 0 ? 4 : 3;
     static constexpr int single() {
         return (kModels != 0u && (kModels & (kModels - 1u)) == 0u) ? __builtin_ctz(kModels) : -1;
     }
@@ -691,7 +695,7 @@ __device__ __forceinline__ void generator_steps(const NetDev &n, int g, int B, i
 
 // One block of B steps starting toff steps after the run call's first step.
 template <class S>
-__global__ void __launch_bounds__(256, 3) k_update(const __grid_constant__ NetDev n, int B, int toff) {
+__global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_constant__ NetDev n, int B, int toff) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int reg_blocks = (n.N_upd + (int)blockDim.x - 1) / (int)blockDim.x;
     const bool gen_block = (int)blockIdx.x >= reg_blocks;
@@ -1716,12 +1720,16 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     }
     if ((uint64_t)e->Wt * 32ull > 0xFFFFFFFFull) return bail(fail(NBG_ERR_UNSUPPORTED, "too many synapses"));
 
-    {   // update-kernel instance: the models present and whether anything learns
+    {   // update-kernel instance: the models the update threads meet (generator
+        // layers have their own threads) and whether anything learns
         unsigned models = 0u;
-        for (const LayerDev &L : e->layers) models |= 1u << L.model;
+        for (const LayerDev &L : e->layers)
+            if (!L.generator) models |= 1u << L.model;
         const unsigned lif_poisson = (1u << NBG_MODEL_LIF_VJ) | (1u << NBG_MODEL_POISSON);
         if (models == (1u << NBG_MODEL_IZH_RK4) && e->plastic)
             e->update_kernel = k_update<Spec<1u << NBG_MODEL_IZH_RK4, 1>>;
+        else if (models == (1u << NBG_MODEL_LIF_VJ) && !e->plastic)
+            e->update_kernel = k_update<Spec<1u << NBG_MODEL_LIF_VJ, 0>>;
         else if ((models & ~lif_poisson) == 0u && !e->plastic)
             e->update_kernel = k_update<Spec<lif_poisson, 0>>;
         else
