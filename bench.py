@@ -60,7 +60,7 @@ BYTES_PER_POST_UPDATE = 36
 KUPDATE_TRAFFIC_BYTES = 63.0e6
 # DRAM bytes (read + write) of one k_update launch of the 256-instance batched
 # workload (15 steps), scaled from an ncu capture on its first 32 instances
-BATCHED_TRAFFIC_BYTES = None
+BATCHED_TRAFFIC_BYTES = 2.206e9  # 238.3 MB on 282,235 LIF neurons x 2,612,540 / 282,235
 # DRAM bytes (read + write) of one dense step launch (64 x 8192, delivery and
 # update) from an ncu capture with a cold L2
 DENSE_TRAFFIC_BYTES = 277.5e6
@@ -308,7 +308,8 @@ def bench_batched(args) -> dict:
                     "sim_steps_per_step": cfg.steps, "block_steps": block_steps, "tuned": tune["choice"],
                     "host_build_s": build_s},
                    neuron_steps_per_s=n_lif * cfg.steps * args.steps / dev,
-                   roofline={"bound": "hbm", "kernel": "k_update<Spec<9, 0>> (LIF + inline Poisson, static)",
+                   roofline={"bound": "hbm", "kernel": "k_update<Spec<1, 0>> (LIF, static; Poisson generators packed "
+                                                       "eight per thread)",
                              "achieved": upd_bytes / dev / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": upd_bytes / dev / 1e9 / peak, "peak_kind": kind,
                              "traffic": (BATCHED_TRAFFIC_BYTES if args.instances == 256 else None),
