@@ -313,7 +313,6 @@ __device__ __forceinline__ void stdp_batch(const NetDev &n, const int (&s)[K], c
 // Arrivals of one target are applied one at a time (a wider batch raises the
 // update kernel's register count past its occupancy target); the rarer
 // post-synaptic pass batches kPostChunk synapses per lane.
-constexpr int kArrivalChunk = 1;
 constexpr int kPostChunk = 2;
 
 // This lane's share of a post-synaptic STDP pass over in-synapses
@@ -400,18 +399,7 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, N
 template <class S>
 __device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
                                            float &acc_b, bool gate, unsigned int word, int first, int t) {
-    while (word) {
-        int sp[kArrivalChunk];
-#pragma unroll
-        for (int k = 0; k < kArrivalChunk; ++k) {
-            sp[k] = first;
-            if (word) {
-                sp[k] = first + __ffs(word) - 1;
-                word &= word - 1u;
-                apply_arrival<S>(n, M, r, acc_a, acc_b, gate, sp[k], t);
-            }
-        }
-    }
+    for (; word; word &= word - 1u) apply_arrival<S>(n, M, r, acc_a, acc_b, gate, first + __ffs(word) - 1, t);
 }
 
 __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t) {
@@ -584,8 +572,6 @@ struct GenIn {
 // Advance every neuron B steps (drain arrivals, integrate, compact spikes,
 // post-synaptic STDP).  One thread per neuron; all lanes stay in the loop so
 // the per-step warp collectives are full-warp.
-//   * the noise currents of the block are drawn up front (independent hash
-//     chains, so they overlap instead of lengthening the per-step chain);
 //   * the first kPrefetch mask words of step b+1 are loaded while step b runs
 //     (every mark for the block's slots was made by earlier launches);
 //   * the post-synaptic STDP pass of a spiking neuron is spread over its warp:

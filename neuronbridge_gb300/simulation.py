@@ -238,7 +238,9 @@ class Simulation:
         if steps <= 0:
             raise ValueError("Simulation.run steps must be positive")
         self.init()
+        t0 = self.next_time
         _lib.check(self.lib.nbg_run(self._h, steps))
+        self._account(self.next_time - t0)
         if self._monitor is not None:
             self._monitor.capture(self.next_time - 1)
         return self
@@ -272,6 +274,18 @@ class Simulation:
         if self._monitor is not None:
             self._monitor.close()
             self._monitor = None
+        return self
+
+    def flush(self) -> "Simulation":
+        """The reference's Simulation.flush: write out the debug monitor's
+        buffered rows."""
+        return self.flush_debug_monitor()
+
+    def publish_output(self) -> "Simulation":
+        """The reference's publish_output pushes output spikes to its
+        attached output drivers (ZeroMQ, arrays); this engine has none, and
+        output_spikes() already holds every output spike, so there is nothing
+        to push."""
         return self
 
     def flush_debug_monitor(self) -> "Simulation":
@@ -601,10 +615,33 @@ class Simulation:
         return t, c, w
 
     def bench_profiling_snapshot(self) -> dict:
-        """Device timings of the last run call (CUDA events on the engine stream)."""
+        """Device timings (CUDA events on the engine stream): the last run
+        call's, and the totals since construction or reset_bench_profiling.
+        The reference's snapshot splits its host event loop into phases
+        (python/bindings/neuronbridge_core.cpp:40-90); this engine has no host
+        loop, so the figures are the device time of the step loop."""
         tot, upd, prop = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         n = ctypes.c_int64()
         _lib.check(self.lib.nbg_profile(self._h, ctypes.byref(tot), ctypes.byref(upd), ctypes.byref(prop),
                                         ctypes.byref(n)))
+        acc = getattr(self, "_prof_total", None) or {"total_device_ms": 0.0, "total_kernel_launches": 0,
+                                                     "run_calls": 0, "simulated_steps": 0}
         return {"device_ms": tot.value, "update_kernel_ms": upd.value, "propagate_kernel_ms": prop.value,
-                "kernel_launches": n.value}
+                "kernel_launches": n.value, **acc}
+
+    def reset_bench_profiling(self) -> "Simulation":
+        """Zero the totals of bench_profiling_snapshot."""
+        self._prof_total = {"total_device_ms": 0.0, "total_kernel_launches": 0, "run_calls": 0,
+                            "simulated_steps": 0}
+        return self
+
+    def _account(self, steps: int) -> None:
+        if getattr(self, "_prof_total", None) is None:
+            self.reset_bench_profiling()
+        tot, n = ctypes.c_double(), ctypes.c_int64()
+        _lib.check(self.lib.nbg_profile(self._h, ctypes.byref(tot), None, None, ctypes.byref(n)))
+        acc = self._prof_total
+        acc["total_device_ms"] += tot.value
+        acc["total_kernel_launches"] += n.value
+        acc["run_calls"] += 1
+        acc["simulated_steps"] += steps

@@ -317,3 +317,19 @@ def test_dense_profile_stdp_uses_device_expf(oracle_lib):
     assert _raster_equal(dense.spike_raster(), _oracle_raster(o, net))
     assert np.array_equal(dense.weights()["weight"], o.weights()[0].astype(np.float32))
     assert not np.array_equal(dense.weights()["weight"], net.to_native().weight)
+
+
+def test_bench_profiling_totals_and_reset():
+    net, cfg = workloads.plain_lif(n=200, steps=100)
+    sim = nb.Simulation(net, cfg)
+    sim.run(300)
+    first = sim.bench_profiling_snapshot()["device_ms"]
+    sim.run(200)
+    p = sim.bench_profiling_snapshot()
+    assert p["run_calls"] == 2 and p["simulated_steps"] == 501
+    assert abs(p["total_device_ms"] - (first + p["device_ms"])) < 1e-9
+    assert p["total_kernel_launches"] >= 2
+    sim.reset_bench_profiling()
+    z = sim.bench_profiling_snapshot()
+    assert z["run_calls"] == 0 and z["total_device_ms"] == 0.0
+    assert sim.publish_output() is sim and sim.flush() is sim
