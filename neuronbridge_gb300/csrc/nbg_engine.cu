@@ -578,6 +578,11 @@ struct GenIn {
 //     the 32 lanes stride over that neuron's CSC list.
 constexpr int kPrefetch = 4; // mask words per neuron prefetched one step ahead
 
+// x mod D for x < 2D: ring slots are advanced by adding and wrapping once
+// instead of an integer division per step and per mark (every step and
+// delay offset added to a slot is below D: B + d_max <= D).
+__device__ __forceinline__ unsigned int wrap_slot(unsigned int x, unsigned int D) { return x >= D ? x - D : x; }
+
 // Bits [woff, woff+nw) of a summary row (nw <= 32), as an nw-bit mask.
 __device__ __forceinline__ unsigned int summary_bits(const unsigned int *srow, int woff, int nw) {
     const int w0 = woff >> 5, sh = woff & 31;
@@ -762,12 +767,13 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     // made by earlier launches, so both are final).
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
     const unsigned int D = (unsigned int)n.D;
+    const unsigned int slot0 = (unsigned int)T0 % D; // the block's first slot; later ones by wrap_slot
     unsigned int sb_cur = 0u, sb_nxt = 0u;
     unsigned int w_cur[kPrefetch] = {0u, 0u, 0u, 0u};
     if (active && fast && nw > 0) {
-        sb_cur = summary_bits(n.wsum + (size_t)((unsigned int)T0 % D) * n.Ws, woff, nw);
-        if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)((unsigned int)(T0 + 1) % D) * n.Ws, woff, nw);
-        const unsigned int *r0 = n.mask + (size_t)((unsigned int)T0 % D) * n.Wt + woff;
+        sb_cur = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
+        if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
+        const unsigned int *r0 = n.mask + (size_t)slot0 * n.Wt + woff;
 #pragma unroll
         for (int k = 0; k < kPrefetch; ++k)
             if ((sb_cur >> k) & 1u) w_cur[k] = r0[k];
@@ -778,7 +784,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
         const int t = T0 + b;
         bool spk = false;
         if (active) {
-            const unsigned int slot = (unsigned int)t % D;
+            const unsigned int slot = wrap_slot(slot0 + (unsigned int)b, D);
             unsigned int *mrow = n.mask + (size_t)slot * n.Wt + woff;
             float acc_a = 0.0f, acc_b = 0.0f;
             const bool gate = r.last > L.ip;
@@ -789,12 +795,12 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                 for (int k = 0; k < kPrefetch; ++k) wc[k] = w_cur[k];
                 // prefetch: flagged words of step b+1, summary of step b+2
                 if (b + 1 < B) {
-                    const unsigned int *rn = n.mask + (size_t)((unsigned int)(t + 1) % D) * n.Wt + woff;
+                    const unsigned int *rn = n.mask + (size_t)wrap_slot(slot + 1u, D) * n.Wt + woff;
 #pragma unroll
                     for (int k = 0; k < kPrefetch; ++k) w_cur[k] = ((sb_nxt >> k) & 1u) ? rn[k] : 0u;
                     sb_cur = sb_nxt;
                     sb_nxt = (b + 2 < B && nw > 0)
-                                 ? summary_bits(n.wsum + (size_t)((unsigned int)(t + 2) % D) * n.Ws, woff, nw)
+                                 ? summary_bits(n.wsum + (size_t)wrap_slot(slot + 2u, D) * n.Ws, woff, nw)
                                  : 0u;
                 }
                 // generator arrivals of this step (pure functions of source and time)
@@ -918,7 +924,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             const unsigned int dl = n.out_delay[q];
             const unsigned int wd = bit >> 5;
             for (unsigned int m = steps; m; m &= m - 1u) {
-                const unsigned int slot = ((unsigned int)T0 + (unsigned int)(__ffs(m) - 1) + dl) % (unsigned int)n.D;
+                const unsigned int slot = wrap_slot(slot0 + (unsigned int)(__ffs(m) - 1) + dl, D);
                 atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
                 atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
             }
