@@ -64,6 +64,29 @@ nbg_status nbg_lif_adjoint_step(const float *g_ext, const float *g_read, float c
                                 float *g_alpha, const float *alpha, const float *theta, const nbg_lif_grad_params *p,
                                 int B, int N, void *stream);
 
+/* The recurrent product of the adjoint, g_ext = dI_{t+1} W_rec^T, on the
+ * tensor cores in split BF16 (x = x_hi + x_lo, three BF16 products
+ * accumulated in FP32, about 16 mantissa bits of each operand), for
+ * B = 128 rows and N a multiple of 128:
+ *   nbg_adjoint_rec_prepare   W_rec (N x N FP32) -> w_hi, w_lo (N x N BF16
+ *                             each, blocked; once per backward)
+ *   nbg_lif_adjoint_step_split  nbg_lif_adjoint_step with g_ext the sum, in
+ *                             order, of n_parts consecutive B x N partials
+ *                             (NULL: none), also writing dI as dI_hi, dI_lo
+ *                             (B x N BF16 each, blocked)
+ *   nbg_adjoint_rec_grad      g_parts[split][B][N] = the split-K partials of
+ *                             dI W_rec^T from those operands; *err gets 4 if
+ *                             a bounded wait of the kernel gave up
+ * There is no counterpart in the reference (it has no gradient path). */
+nbg_status nbg_adjoint_rec_prepare(const float *w_rec, void *w_hi, void *w_lo, int N, void *stream);
+nbg_status nbg_lif_adjoint_step_split(const float *g_parts, int n_parts, const float *g_read, float c_t,
+                                      const float *u, const float *s, const uint8_t *m, const float *vprev,
+                                      float *lam_v, float *dI, void *dI_hi, void *dI_lo, float *g_theta,
+                                      float *g_alpha, const float *alpha, const float *theta,
+                                      const nbg_lif_grad_params *p, int B, int N, void *stream);
+nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *dI_hi, const void *dI_lo,
+                                float *g_parts, int split, int B, int N, int *err, void *stream);
+
 /* Poisson input spikes x[t][b][c] in {0, 1}: channel c fires with
  * probability min(1, rate_c * dt * 1e-3) from the PoissonRate hash of
  * (seed-offset index b*C + c + seed, step t). */

@@ -50,6 +50,10 @@ _SIG = {
     "nbg_lif_forward_step_sparse": (ctypes.c_int, [_vp] * 13 + [ctypes.c_float, _vp, _vp, ctypes.POINTER(GradParams),
                                                                 ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_spike_lists": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "nbg_adjoint_rec_prepare": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),
+    "nbg_lif_adjoint_step_split": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_float] + [_vp] * 12 +
+                                   [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp]),
+    "nbg_adjoint_rec_grad": (ctypes.c_int, [_vp] * 5 + [ctypes.c_int] * 3 + [_vp, _vp]),
 }
 _LIB = None
 
@@ -111,6 +115,16 @@ class _SpikeLists:
 
 def _sparse_ok(p, N: int) -> bool:
     return not p.smooth and N <= 2048
+
+
+# The recurrent product dI_{t+1} W_rec^T of the adjoint runs on the tensor
+# cores (split BF16, nbg_adjoint_rec_grad) for B = 128 rows and N a multiple
+# of 128 in spiking mode; its split-K partials are added by the next step.
+TC_SPLIT = 8
+
+
+def _tc_ok(p, B: int, N: int) -> bool:
+    return not p.smooth and B == 128 and N % 128 == 0
 
 
 def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out):
@@ -178,6 +192,16 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     have_next = False
     sparse = _sparse_ok(p, N)
     lists = _SpikeLists(B, N, x.device) if sparse else None
+    tc = _tc_ok(p, B, N)
+    if tc:
+        w_hi = torch.empty(N * N, device=x.device, dtype=torch.bfloat16)
+        w_lo = torch.empty(N * N, device=x.device, dtype=torch.bfloat16)
+        d_hi = torch.empty(B * N, device=x.device, dtype=torch.bfloat16)
+        d_lo = torch.empty(B * N, device=x.device, dtype=torch.bfloat16)
+        split = min(TC_SPLIT, N // 64)
+        g_parts = torch.empty((split, B, N), device=x.device, dtype=torch.float32)
+        tc_err = torch.zeros(1, device=x.device, dtype=torch.int32)
+        _lib.check(lib.nbg_adjoint_rec_prepare(_ptr(w_rec), _ptr(w_hi), _ptr(w_lo), N, st))
     segments = list(enumerate(range(0, T, K)))
     for seg, t0 in reversed(segments):
         t1 = min(T, t0 + K)
@@ -198,6 +222,15 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                                                 ctypes.byref(p), B, N, st))
         for k in reversed(range(L)):
             t = t0 + k
+            if tc:  # g_parts holds dI_{t+1} W_rec^T from the previous iteration
+                _lib.check(lib.nbg_lif_adjoint_step_split(
+                    _ptr(g_parts) if have_next else None, split, _ptr(g_read), float(coef[t]), _ptr(U[k]),
+                    _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]), _ptr(lam_v), _ptr(dI[k]), _ptr(d_hi), _ptr(d_lo),
+                    _ptr(g_theta), _ptr(g_alpha), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
+                _lib.check(lib.nbg_adjoint_rec_grad(_ptr(w_hi), _ptr(w_lo), _ptr(d_hi), _ptr(d_lo), _ptr(g_parts),
+                                                    split, B, N, _ptr(tc_err), st))
+                have_next = True
+                continue
             ge = None
             if have_next:  # dL/ds_t from the recurrent path: dI_{t+1} W_rec^T
                 torch.mm(dI_next if k == L - 1 else dI[k + 1], w_rec.t(), out=g_ext)
@@ -210,7 +243,13 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
         g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
         dI_next.copy_(dI[0])
-    return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0)
+    return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), (tc_err if tc else None)
+
+
+def _check_tc(err) -> None:
+    """Raise if a bounded wait of the tensor-core recurrent product gave up."""
+    if err is not None and int(err.item()) != 0:
+        raise RuntimeError("nbg_adjoint_rec_grad: a tensor-core wait timed out; the gradients are invalid")
 
 
 class _GraphPlan:
@@ -280,7 +319,8 @@ class _GraphPlan:
                 lib, self.gy, self.x, w_in, w_rec, w_out, alpha, theta, self.z, self.ck_v, self.ck_ref, self.ck_s,
                 self.p, self.K, self.coef))
         self.bwd.replay()
-        return tuple(g.clone() for g in self.grads)
+        _check_tc(self.grads[5])
+        return tuple(g.clone() for g in self.grads[:5])
 
 
 class _Recurrence(torch.autograd.Function):
@@ -320,8 +360,9 @@ class _Recurrence(torch.autograd.Function):
         if plan is not None:
             grads = plan.backward(ctx.owner, gy, x, ctx.ck + (z,))
         else:
-            grads = _backward_body(_bind(), gy, x, w_in, w_rec, w_out, alpha, theta, z, *ctx.ck, cfg["params"],
-                                   cfg["checkpoint"], cfg["coef"])
+            *grads, err = _backward_body(_bind(), gy, x, w_in, w_rec, w_out, alpha, theta, z, *ctx.ck, cfg["params"],
+                                         cfg["checkpoint"], cfg["coef"])
+            _check_tc(err)
         return (None, *grads, None)
 
 

@@ -8,14 +8,11 @@
 #include <cuda_runtime.h>
 
 #include "nbg_adjoint.h"
+#include "nbg_lif_grad.cuh"
 #include "nbg_common.cuh"
 
 namespace {
 
-__device__ __forceinline__ float surrogate(float x, float k) {
-    const float d = 1.0f + k * fabsf(x);
-    return 1.0f / (d * d);
-}
 
 __global__ void __launch_bounds__(256) k_lif_fwd(const float *__restrict__ I, float *__restrict__ v,
                                                  int *__restrict__ ref, float *__restrict__ s_out,

@@ -1,0 +1,253 @@
+// nbg_adjoint_tc.cu -- the recurrent product of the adjoint on tcgen05
+// (C ABI in include/nbg_adjoint.h).
+//
+// Each adjoint step needs g_ext[b][i] = sum_j dI[b][j] W_rec[i][j], a GEMM of
+// B = 128 rows by N by N.  As cuBLAS FP32 it takes about 24 us at N = 1024;
+// here it runs on the tensor cores in split BF16:
+//   x = x_hi + x_lo,  x_hi = bf16(x),  x_lo = bf16(x - x_hi)
+//   dI W^T ~= dI_hi W_hi^T + dI_hi W_lo^T + dI_lo W_hi^T      (FP32 accumulation)
+// which keeps about 16 mantissa bits of each operand (the dropped term
+// dI_lo W_lo^T is below 2^-16 of the product).
+//
+// Operands use the UMMA blocked K-major layout of nbg_umma.cuh: A = W (rows
+// i, K = j), tiled once per backward by nbg_adjoint_rec_prepare; B = dI
+// (rows b, K = j), written tiled by the adjoint step itself
+// (nbg_lif_adjoint_step_split).  One CTA owns 128 rows i and all 128 batch
+// rows (UMMA M = N = 128, a 128-column TMEM accumulator) over one K range;
+// the split-K partials go to g_parts[ks] and the next adjoint step adds them
+// in a fixed order, so the backward stays deterministic.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "nbg_adjoint.h"
+#include "nbg_common.cuh"
+#include "nbg_lif_grad.cuh"
+#include "nbg_umma.cuh"
+
+namespace {
+
+using namespace umma;
+
+constexpr int kAdjM = 128, kAdjN = 128;
+constexpr int kAdjStages = 3;
+constexpr int kAdjBlockA = kAdjM * kKChunk * 2; // 16 KiB per operand block
+constexpr int kAdjBlockB = kAdjN * kKChunk * 2;
+constexpr int kAdjStageBytes = 2 * kAdjBlockA + 2 * kAdjBlockB; // A_hi A_lo B_hi B_lo
+constexpr int kAdjSmemBytes = kAdjStages * kAdjStageBytes + 1024 + 256;
+constexpr int kAdjTmemCols = 128;
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> F32, K-major, M = N = 128.
+constexpr uint32_t kAdjIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kAdjN >> 3) << 17) |
+                               ((uint32_t)(kAdjM >> 4) << 24);
+
+// Element (r, c) of a rows x cols matrix in the blocked layout of 128-row x
+// 64-column blocks, block (r / 128, c / 64) at ((r / 128) * (cols / 64) +
+// c / 64) blocks.
+__device__ __forceinline__ size_t blocked_index(int r, int c, int cols) {
+    const size_t blk = (size_t)(r >> 7) * (size_t)(cols >> 6) + (size_t)(c >> 6);
+    return blk * (size_t)(kAdjM * kKChunk) + block_offset(r & 127, c & 63) / 2;
+}
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+    hi = __float2bfloat16_rn(x);
+    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+__global__ void k_split_blocked(const float *__restrict__ x, __nv_bfloat16 *__restrict__ hi,
+                                __nv_bfloat16 *__restrict__ lo, int rows, int cols) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)rows * cols) return;
+    const int r = (int)(idx / cols), c = (int)(idx % cols);
+    const size_t o = blocked_index(r, c, cols);
+    split_bf16(x[idx], hi[o], lo[o]);
+}
+
+// The adjoint step of k_lif_adj (nbg_adjoint.cu) with g_ext the fixed-order
+// sum of the split-K partials, writing dI also as the split BF16 B operand.
+__global__ void __launch_bounds__(256) k_lif_adj_split(
+    const float *__restrict__ g_parts, int n_parts, const float *__restrict__ g_read, float c_t,
+    const float *__restrict__ u, const float *__restrict__ s, const unsigned char *__restrict__ m,
+    const float *__restrict__ vprev, float *__restrict__ lam_v, float *__restrict__ dI,
+    __nv_bfloat16 *__restrict__ dI_hi, __nv_bfloat16 *__restrict__ dI_lo, float *__restrict__ g_theta,
+    float *__restrict__ g_alpha, const float *__restrict__ alpha, const float *__restrict__ theta,
+    nbg_lif_grad_params p, int N, int total) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int j = idx % N;
+    const float uu = u[idx], ss = s[idx], lv = lam_v[idx];
+    const float th = theta[j];
+    const float dsdu = p.smooth ? p.slope * ss * (1.0f - ss) : surrogate(uu - th, p.slope);
+    float gs = c_t * g_read[idx] - lv * (uu - p.v_reset);
+    if (g_parts) {
+        float ge = g_parts[idx];
+        for (int q = 1; q < n_parts; ++q) ge = ge + g_parts[(size_t)q * total + idx];
+        gs = gs + ge;
+    }
+    const float gu = gs * dsdu + lv * (1.0f - ss);
+    const float gm = m[idx] ? gu : 0.0f;
+    dI[idx] = gm;
+    const size_t o = blocked_index(idx / N, j, N);
+    split_bf16(gm, dI_hi[o], dI_lo[o]);
+    lam_v[idx] = gm * (1.0f - alpha[j]);
+    g_theta[idx] = g_theta[idx] - gs * dsdu;
+    g_alpha[idx] = g_alpha[idx] + gm * (p.v_rest - vprev[idx]);
+}
+
+// g_parts[ks][b][i] = sum over the K chunks of split ks of the three split
+// products.  Grid (N / 128, split), 256 threads: warp 0 lane 0 produces
+// (bulk copies into kAdjStages stages), warp 1 lane 0 issues the MMAs, warp 2
+// owns the TMEM allocation, all 8 warps run the epilogue.  Every mbarrier
+// wait is bounded; on expiry the CTA records kUmmaTimeout in *err, stops,
+// frees its TMEM and returns.
+__global__ void __launch_bounds__(kThreads, 1)
+    k_adj_umma(const __nv_bfloat16 *__restrict__ w_hi, const __nv_bfloat16 *__restrict__ w_lo,
+               const __nv_bfloat16 *__restrict__ d_hi, const __nv_bfloat16 *__restrict__ d_lo,
+               float *__restrict__ g_parts, int n, int split, int *__restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(stages + kAdjStages * kAdjStageBytes);
+    uint64_t *empty = full + kAdjStages;
+    uint64_t *done = empty + kAdjStages;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *abort = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = blockIdx.x, ks = blockIdx.y;
+    const int kchunks = n / kKChunk;
+    const int per = kchunks / split;
+    const int kc0 = ks * per;
+    const int iters = (ks == split - 1) ? kchunks - kc0 : per;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kAdjStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(kAdjTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) { // producer
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % kAdjStages;
+            if (it >= kAdjStages && !mbar_wait(&empty[s], ((it / kAdjStages) & 1) ^ 1, abort)) break;
+            uint8_t *st = stages + s * kAdjStageBytes;
+            const int kc = kc0 + it;
+            const size_t a_blk = (size_t)mt * kchunks + kc;
+            mbar_expect_tx(&full[s], kAdjStageBytes);
+            bulk_copy(st, (const uint8_t *)w_hi + a_blk * kAdjBlockA, kAdjBlockA, &full[s]);
+            bulk_copy(st + kAdjBlockA, (const uint8_t *)w_lo + a_blk * kAdjBlockA, kAdjBlockA, &full[s]);
+            bulk_copy(st + 2 * kAdjBlockA, (const uint8_t *)d_hi + (size_t)kc * kAdjBlockB, kAdjBlockB, &full[s]);
+            bulk_copy(st + 2 * kAdjBlockA + kAdjBlockB, (const uint8_t *)d_lo + (size_t)kc * kAdjBlockB, kAdjBlockB,
+                      &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) { // MMA issuer
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % kAdjStages;
+            if (!mbar_wait(&full[s], (it / kAdjStages) & 1, abort)) break;
+            fence_after();
+            const uint32_t a_hi = smem_addr(stages + s * kAdjStageBytes);
+            const uint32_t a_lo = a_hi + kAdjBlockA;
+            const uint32_t b_hi = a_hi + 2 * kAdjBlockA;
+            const uint32_t b_lo = b_hi + kAdjBlockB;
+#pragma unroll
+            for (int k = 0; k < kKChunk / 16; ++k) {
+                mma(tmem, make_desc(a_hi + 256 * k), make_desc(b_hi + 256 * k), kAdjIdesc, (it | k) != 0);
+                mma(tmem, make_desc(a_lo + 256 * k), make_desc(b_hi + 256 * k), kAdjIdesc, 1u);
+                mma(tmem, make_desc(a_hi + 256 * k), make_desc(b_lo + 256 * k), kAdjIdesc, 1u);
+            }
+            commit(&empty[s]);
+        }
+        commit(done);
+    }
+    __syncwarp();
+    // epilogue: warp w reads TMEM lanes 32*(w%4).. (rows i) and columns
+    // 64*(w/4).. (batch rows b)
+    mbar_wait(done, 0, abort);
+    __syncthreads();
+    fence_after();
+    const int q = warp & 3, h = warp >> 2;
+    const int i = mt * kAdjM + 32 * q + lane;
+    if (!*abort) {
+        float *out = g_parts + (size_t)ks * kAdjN * n;
+#pragma unroll
+        for (int c16 = 0; c16 < 4; ++c16) {
+            float acc[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * h + 16 * c16), acc);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) out[(size_t)(64 * h + 16 * c16 + c) * n + i] = acc[c];
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort) atomicOr(err, kUmmaTimeout);
+    if (warp == 2) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kAdjTmemCols)
+                     : "memory");
+    }
+}
+
+bool adj_shape_ok(int B, int N) { return B == kAdjN && N > 0 && N % kAdjM == 0; }
+
+} // namespace
+
+extern "C" {
+
+nbg_status nbg_adjoint_rec_prepare(const float *w_rec, void *w_hi, void *w_lo, int N, void *stream) {
+    if (!w_rec || !w_hi || !w_lo || N <= 0 || N % kAdjM)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_rec_prepare: N must be a positive multiple of %d", kAdjM);
+    const long long total = (long long)N * N;
+    k_split_blocked<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        w_rec, (__nv_bfloat16 *)w_hi, (__nv_bfloat16 *)w_lo, N, N);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_lif_adjoint_step_split(const float *g_parts, int n_parts, const float *g_read, float c_t,
+                                      const float *u, const float *s, const uint8_t *m, const float *vprev,
+                                      float *lam_v, float *dI, void *dI_hi, void *dI_lo, float *g_theta,
+                                      float *g_alpha, const float *alpha, const float *theta,
+                                      const nbg_lif_grad_params *p, int B, int N, void *stream) {
+    if (!g_read || !u || !s || !m || !vprev || !lam_v || !dI || !dI_hi || !dI_lo || !g_theta || !g_alpha || !alpha ||
+        !theta || !p || (g_parts && n_parts <= 0) || !adj_shape_ok(B, N))
+        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_adjoint_step_split: bad arguments (B must be %d, N a multiple of %d)",
+                        kAdjN, kAdjM);
+    const int total = B * N;
+    k_lif_adj_split<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
+        g_parts, n_parts, g_read, c_t, u, s, m, vprev, lam_v, dI, (__nv_bfloat16 *)dI_hi, (__nv_bfloat16 *)dI_lo,
+        g_theta, g_alpha, alpha, theta, *p, N, total);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *dI_hi, const void *dI_lo,
+                                float *g_parts, int split, int B, int N, int *err, void *stream) {
+    if (!w_hi || !w_lo || !dI_hi || !dI_lo || !g_parts || !err || !adj_shape_ok(B, N) || split <= 0 ||
+        split > N / kKChunk)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_rec_grad: bad arguments (B must be %d, N a multiple of %d, "
+                        "1 <= split <= N / %d)", kAdjN, kAdjM, kKChunk);
+    static bool attr_set = false;
+    if (!attr_set) {
+        NBG_CUDA(cudaFuncSetAttribute(k_adj_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmemBytes));
+        attr_set = true;
+    }
+    k_adj_umma<<<dim3(N / kAdjM, split), kThreads, kAdjSmemBytes, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo, (const __nv_bfloat16 *)dI_hi,
+        (const __nv_bfloat16 *)dI_lo, g_parts, N, split, err);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+} // extern "C"
