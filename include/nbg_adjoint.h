@@ -87,6 +87,27 @@ nbg_status nbg_lif_adjoint_step_split(const float *g_parts, int n_parts, const f
 nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *dI_hi, const void *dI_lo,
                                 float *g_parts, int split, int B, int N, int *err, void *stream);
 
+/* The recurrent weight gradient of a checkpoint segment on the tensor cores,
+ * dW_rec += sum over its L steps of S_{t-1}^T dI_t, in three calls:
+ *   nbg_adjoint_blocked_t   src [L][B][R] FP32 -> the R x (L*B) matrix, row r,
+ *                           column l*B + b, blocked BF16; split into hi and lo
+ *                           when lo is not NULL (else the values must be
+ *                           exact in BF16, as spikes are).  R a multiple of
+ *                           128, L*B of 64.
+ *   nbg_adjoint_wgrad       part[split][Nc][M] = split-K partials of
+ *                           (a_hi + a_lo)(b + b_lo)^T without the lo x lo
+ *                           term (b_lo NULL: b exact), a: M x K, b: Nc x K (from
+ *                           nbg_adjoint_blocked_t), M a multiple of 128, Nc
+ *                           of 256, K of 64; *err gets 4 if a bounded wait
+ *                           gave up
+ *   nbg_adjoint_reduce_add  g[e] += sum over q, in order, of part[q][e]
+ * With a = dI^T (split) and b = S^T (or X^T, split) part[q] is laid out as
+ * dW_rec (or dW_in): row = presynaptic neuron (or input channel). */
+nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, void *hi, void *lo, void *stream);
+nbg_status nbg_adjoint_wgrad(const void *a_hi, const void *a_lo, const void *b, const void *b_lo, int M, int Nc,
+                             int K, float *part, int split, int *err, void *stream);
+nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_t count, void *stream);
+
 /* Poisson input spikes x[t][b][c] in {0, 1}: channel c fires with
  * probability min(1, rate_c * dt * 1e-3) from the PoissonRate hash of
  * (seed-offset index b*C + c + seed, step t). */

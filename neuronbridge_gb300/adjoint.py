@@ -54,6 +54,10 @@ _SIG = {
     "nbg_lif_adjoint_step_split": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_float] + [_vp] * 12 +
                                    [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_adjoint_rec_grad": (ctypes.c_int, [_vp] * 5 + [ctypes.c_int] * 3 + [_vp, _vp]),
+    "nbg_adjoint_blocked_t": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "nbg_adjoint_wgrad": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
+                                         ctypes.c_int, _vp, _vp]),
+    "nbg_adjoint_reduce_add": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int64, _vp]),
 }
 _LIB = None
 
@@ -121,6 +125,11 @@ def _sparse_ok(p, N: int) -> bool:
 # cores (split BF16, nbg_adjoint_rec_grad) for B = 128 rows and N a multiple
 # of 128 in spiking mode; its split-K partials are added by the next step.
 TC_SPLIT = 8
+# The segment's weight gradients S^T dI (spikes exact in BF16) and X^T dI
+# (inputs split like dI) on the tensor cores as well when N (and C) are
+# multiples of 256; split-K partials.
+WGRAD_SPLIT = 4
+WGRAD_IN_SPLIT = 16
 
 
 def _tc_ok(p, B: int, N: int) -> bool:
@@ -202,6 +211,18 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         g_parts = torch.empty((split, B, N), device=x.device, dtype=torch.float32)
         tc_err = torch.zeros(1, device=x.device, dtype=torch.int32)
         _lib.check(lib.nbg_adjoint_rec_prepare(_ptr(w_rec), _ptr(w_hi), _ptr(w_lo), N, st))
+    tc_w = tc and N % 256 == 0
+    if tc_w:
+        kk_max = L_max * B
+        dT_hi = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
+        dT_lo = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
+        sT = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
+        tc_in = C % 256 == 0
+        w_part = torch.empty(max(WGRAD_SPLIT * N * N, WGRAD_IN_SPLIT * C * N if tc_in else 0), device=x.device,
+                             dtype=torch.float32)
+        if tc_in:
+            xT_hi = torch.empty(C * kk_max, device=x.device, dtype=torch.bfloat16)
+            xT_lo = torch.empty(C * kk_max, device=x.device, dtype=torch.bfloat16)
     segments = list(enumerate(range(0, T, K)))
     for seg, t0 in reversed(segments):
         t1 = min(T, t0 + K)
@@ -240,8 +261,23 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                                                 _ptr(dI[k]), _ptr(g_theta), _ptr(g_alpha), _ptr(alpha),
                                                 _ptr(theta), ctypes.byref(p), B, N, st))
             have_next = True
-        g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
-        g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
+        if tc_w:
+            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, _ptr(dT_hi), _ptr(dT_lo), st))
+            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(S), L, B, N, _ptr(sT), None, st))
+            ws = min(WGRAD_SPLIT, L * B // 64)
+            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(sT), None, N, N, L * B, _ptr(w_part), ws,
+                                             _ptr(tc_err), st))
+            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_rec), _ptr(w_part), ws, N * N, st))
+        else:
+            g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
+        if tc_w and tc_in:
+            ws = min(WGRAD_IN_SPLIT, L * B // 64)
+            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x[t0:t1]), L, B, C, _ptr(xT_hi), _ptr(xT_lo), st))
+            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(xT_hi), _ptr(xT_lo), N, C, L * B,
+                                             _ptr(w_part), ws, _ptr(tc_err), st))
+            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_in), _ptr(w_part), ws, C * N, st))
+        else:
+            g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
         dI_next.copy_(dI[0])
     return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), (tc_err if tc else None)
 

@@ -16,6 +16,16 @@
 // rows (UMMA M = N = 128, a 128-column TMEM accumulator) over one K range;
 // the split-K partials go to g_parts[ks] and the next adjoint step adds them
 // in a fixed order, so the backward stays deterministic.
+//
+// The weight gradients of a checkpoint segment, dW_rec = sum_t S_{t-1}^T dI_t
+// and dW_in = sum_t X_t^T dI_t, are the same kind of product with K = the
+// segment's (step, batch row) pairs: D[j][n] = sum_K dI^T[j][K] B[n][K] with
+// dI^T split (two products) and B = S^T or X^T exact in BF16 (spikes are 0 or
+// 1).  nbg_adjoint_blocked_t lays the [L][B][R] FP32 arrays out transposed
+// and blocked, nbg_adjoint_wgrad runs the tcgen05 product (UMMA M = 128 rows
+// j, N = 256 columns n, split-K partials stored as [split][n][j] so the
+// stores are coalesced along j), and nbg_adjoint_reduce_add adds the
+// partials into the gradient in a fixed order.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -199,6 +209,154 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// [L][B][R] FP32 -> the R x (L*B) matrix (row r, K = l*B + b) in the blocked
+// layout, split into hi and lo (lo may be null: the values are exact in BF16).
+__global__ void k_blocked_t(const float *__restrict__ src, int L, int B, int R, __nv_bfloat16 *__restrict__ hi,
+                            __nv_bfloat16 *__restrict__ lo) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)L * B * R;
+    if (idx >= total) return;
+    const int r = (int)(idx % R);
+    const int kk = (int)(idx / R); // l * B + b
+    const size_t o = blocked_index(r, kk, L * B);
+    if (lo) split_bf16(src[idx], hi[o], lo[o]);
+    else hi[o] = __float2bfloat16_rn(src[idx]);
+}
+
+constexpr int kWgN = 256; // UMMA N of the weight-gradient product
+constexpr int kWgBlockB = kWgN * kKChunk * 2; // 32 KiB
+// stages: 3 of A_hi A_lo B (64 KiB), or 2 of A_hi A_lo B_hi B_lo (96 KiB)
+template <bool kSplitB> struct WgShape {
+    static constexpr int stages = kSplitB ? 2 : 3;
+    static constexpr int stage_bytes = 2 * kAdjBlockA + (kSplitB ? 2 : 1) * kWgBlockB;
+    static constexpr int smem_bytes = stages * stage_bytes + 1024 + 256;
+};
+constexpr int kWgTmemCols = 256;
+constexpr uint32_t kWgIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kWgN >> 3) << 17) |
+                              ((uint32_t)(kAdjM >> 4) << 24);
+
+// part[ks][n][j] = sum over the K chunks of split ks of (a_hi + a_lo)[j][K]
+// (b_hi + b_lo)[n][K], the lo x lo product dropped (b_lo absent when b is
+// exact in BF16).  a: M x K blocked (128-row tiles), b: Nc x K blocked (its
+// 256-row tile n0 = blockIdx.y * 256 is two 128-row block rows).  Grid
+// (M / 128, Nc / 256, split); roles as in k_adj_umma.
+template <bool kSplitB>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_wgrad_umma(const __nv_bfloat16 *__restrict__ a_hi, const __nv_bfloat16 *__restrict__ a_lo,
+                 const __nv_bfloat16 *__restrict__ b, const __nv_bfloat16 *__restrict__ b_lo,
+                 float *__restrict__ part, int M, int Nc, int K, int split, int *__restrict__ err) {
+    constexpr int kWgStages = WgShape<kSplitB>::stages;
+    constexpr int kWgStageBytes = WgShape<kSplitB>::stage_bytes;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(stages + kWgStages * kWgStageBytes);
+    uint64_t *empty = full + kWgStages;
+    uint64_t *done = empty + kWgStages;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *abort = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = blockIdx.x, nt = blockIdx.y, ks = blockIdx.z;
+    const int kchunks = K / kKChunk;
+    const int per = kchunks / split;
+    const int kc0 = ks * per;
+    const int iters = (ks == split - 1) ? kchunks - kc0 : per;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kWgStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(kWgTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) { // producer
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % kWgStages;
+            if (it >= kWgStages && !mbar_wait(&empty[s], ((it / kWgStages) & 1) ^ 1, abort)) break;
+            uint8_t *st = stages + s * kWgStageBytes;
+            const int kc = kc0 + it;
+            const size_t a_blk = (size_t)mt * kchunks + kc;
+            const size_t b_blk0 = (size_t)(2 * nt) * kchunks + kc, b_blk1 = (size_t)(2 * nt + 1) * kchunks + kc;
+            mbar_expect_tx(&full[s], kWgStageBytes);
+            bulk_copy(st, (const uint8_t *)a_hi + a_blk * kAdjBlockA, kAdjBlockA, &full[s]);
+            bulk_copy(st + kAdjBlockA, (const uint8_t *)a_lo + a_blk * kAdjBlockA, kAdjBlockA, &full[s]);
+            // the two 128-row halves of the B tile, one after the other: rows
+            // 128..255 continue the 8-row core-matrix groups at byte 16384
+            bulk_copy(st + 2 * kAdjBlockA, (const uint8_t *)b + b_blk0 * kAdjBlockA, kAdjBlockA, &full[s]);
+            bulk_copy(st + 3 * kAdjBlockA, (const uint8_t *)b + b_blk1 * kAdjBlockA, kAdjBlockA, &full[s]);
+            if constexpr (kSplitB) {
+                bulk_copy(st + 4 * kAdjBlockA, (const uint8_t *)b_lo + b_blk0 * kAdjBlockA, kAdjBlockA, &full[s]);
+                bulk_copy(st + 5 * kAdjBlockA, (const uint8_t *)b_lo + b_blk1 * kAdjBlockA, kAdjBlockA, &full[s]);
+            }
+        }
+    } else if (warp == 1 && lane == 0) { // MMA issuer
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % kWgStages;
+            if (!mbar_wait(&full[s], (it / kWgStages) & 1, abort)) break;
+            fence_after();
+            const uint32_t ah = smem_addr(stages + s * kWgStageBytes);
+            const uint32_t al = ah + kAdjBlockA;
+            const uint32_t bb = ah + 2 * kAdjBlockA;
+#pragma unroll
+            for (int k = 0; k < kKChunk / 16; ++k) {
+                mma(tmem, make_desc(ah + 256 * k), make_desc(bb + 256 * k), kWgIdesc, (it | k) != 0);
+                mma(tmem, make_desc(al + 256 * k), make_desc(bb + 256 * k), kWgIdesc, 1u);
+                if constexpr (kSplitB)
+                    mma(tmem, make_desc(ah + 256 * k), make_desc(bb + kWgBlockB + 256 * k), kWgIdesc, 1u);
+            }
+            commit(&empty[s]);
+        }
+        commit(done);
+    }
+    __syncwarp();
+    mbar_wait(done, 0, abort);
+    __syncthreads();
+    fence_after();
+    // epilogue: warp w reads TMEM lanes 32*(w%4).. (rows j) and columns
+    // 128*(w/4).. (n); stores are coalesced along j
+    const int q = warp & 3, h = warp >> 2;
+    const int j = mt * kAdjM + 32 * q + lane;
+    if (!*abort) {
+        float *out = part + (size_t)ks * Nc * M;
+        for (int c16 = 0; c16 < 8; ++c16) {
+            float acc[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(128 * h + 16 * c16), acc);
+            const int n0 = nt * kWgN + 128 * h + 16 * c16;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) out[(size_t)(n0 + c) * M + j] = acc[c];
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort) atomicOr(err, kUmmaTimeout);
+    if (warp == 2) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kWgTmemCols)
+                     : "memory");
+    }
+}
+
+__global__ void k_reduce_add(float *__restrict__ g, const float *__restrict__ part, int split, long long count) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count) return;
+    float acc = part[idx];
+    for (int q = 1; q < split; ++q) acc = acc + part[(size_t)q * count + idx];
+    g[idx] = g[idx] + acc;
+}
+
 bool adj_shape_ok(int B, int N) { return B == kAdjN && N > 0 && N % kAdjM == 0; }
 
 } // namespace
@@ -246,6 +404,54 @@ nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *
     k_adj_umma<<<dim3(N / kAdjM, split), kThreads, kAdjSmemBytes, (cudaStream_t)stream>>>(
         (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo, (const __nv_bfloat16 *)dI_hi,
         (const __nv_bfloat16 *)dI_lo, g_parts, N, split, err);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, void *hi, void *lo, void *stream) {
+    if (!src || !hi || L <= 0 || B <= 0 || R <= 0 || R % kAdjM || ((long long)L * B) % kKChunk)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_blocked_t: R must be a multiple of %d and L*B of %d", kAdjM,
+                        kKChunk);
+    const long long total = (long long)L * B * R;
+    k_blocked_t<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        src, L, B, R, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_adjoint_wgrad(const void *a_hi, const void *a_lo, const void *b, const void *b_lo, int M, int Nc,
+                             int K, float *part, int split, int *err, void *stream) {
+    if (!a_hi || !a_lo || !b || !part || !err || M <= 0 || M % kAdjM || Nc <= 0 || Nc % kWgN || K <= 0 ||
+        K % kKChunk || split <= 0 || split > K / kKChunk)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_wgrad: M must be a multiple of %d, Nc of %d, K of %d, "
+                        "1 <= split <= K / %d", kAdjM, kWgN, kKChunk, kKChunk);
+    static bool attr_set[2] = {false, false};
+    const dim3 grid(M / kAdjM, Nc / kWgN, split);
+    const __nv_bfloat16 *ah = (const __nv_bfloat16 *)a_hi, *al = (const __nv_bfloat16 *)a_lo;
+    if (b_lo) {
+        if (!attr_set[1]) {
+            NBG_CUDA(cudaFuncSetAttribute(k_wgrad_umma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          WgShape<true>::smem_bytes));
+            attr_set[1] = true;
+        }
+        k_wgrad_umma<true><<<grid, kThreads, WgShape<true>::smem_bytes, (cudaStream_t)stream>>>(
+            ah, al, (const __nv_bfloat16 *)b, (const __nv_bfloat16 *)b_lo, part, M, Nc, K, split, err);
+    } else {
+        if (!attr_set[0]) {
+            NBG_CUDA(cudaFuncSetAttribute(k_wgrad_umma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          WgShape<false>::smem_bytes));
+            attr_set[0] = true;
+        }
+        k_wgrad_umma<false><<<grid, kThreads, WgShape<false>::smem_bytes, (cudaStream_t)stream>>>(
+            ah, al, (const __nv_bfloat16 *)b, nullptr, part, M, Nc, K, split, err);
+    }
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_t count, void *stream) {
+    if (!g || !part || split <= 0 || count <= 0) return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_reduce_add: bad arguments");
+    k_reduce_add<<<(unsigned)((count + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g, part, split, (long long)count);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

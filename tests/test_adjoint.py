@@ -168,13 +168,14 @@ def test_reference_dynamics_gradcheck_cpu():
 
 @pytest.mark.gpu
 def test_tensor_core_recurrent_product(monkeypatch):
-    """B = 128 rows and N a multiple of 128 in spiking mode: dI_{t+1} W_rec^T
-    runs on tcgen05 in split BF16.  Gradients stay within the FP64 tolerance
-    of the spiking test and agree with the cuBLAS FP32 path."""
+    """B = 128 rows, N and C multiples of 256, spiking mode: dI_{t+1} W_rec^T
+    and the segments' weight gradients S^T dI and X^T dI run on tcgen05 in
+    split BF16.  Gradients stay within the FP64 tolerance of the spiking test
+    and agree with the cuBLAS FP32 path."""
     from neuronbridge_gb300 import adjoint
     from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
 
-    kw = dict(n_in=16, n_rec=256, n_out=5, checkpoint=20, seed=11)
+    kw = dict(n_in=256, n_rec=256, n_out=5, checkpoint=20, seed=11)  # W_in gradient on the tensor cores too
     torch.manual_seed(0)
     model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, **kw, **SPIKING)
     rates = torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0
