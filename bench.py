@@ -218,18 +218,23 @@ def bench_lif(args) -> dict:
     # device time over its launches is the launch duration
     sim = nb.Simulation(net, cfg)
     tune = _launch_shape(sim, args, 1000)  # launch shape only; resets the simulation
+    trace_ids = np.arange(0, 1000, 100)  # V of neurons 0, 100, ..., 900 every step, with the raster
+    sim.set_trace(trace_ids)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         sim.run(cfg.steps)
         sim.clear_spikes()
         flush.fill_(1.0)
-    ev = dev = upd = 0.0
-    launches = 0
+    ev = dev = upd = wall = 0.0
+    launches = spikes = 0
     clocks = ClockSampler(0)
     clocks.start()
     for _ in range(args.steps):
         e0 = sim.num_events
+        w0 = time.perf_counter()
         sim.run(cfg.steps)
+        wall += time.perf_counter() - w0
+        spikes += len(sim.spike_raster()[0])
         p = sim.bench_profiling_snapshot()
         ev += sim.num_events - e0
         dev += p["device_ms"] / 1e3
@@ -243,11 +248,14 @@ def bench_lif(args) -> dict:
     peak, kind = _peaks()
     return _common(args, "synaptic events/s", ev / dev, "synaptic events/s", 1e3 * dev / args.steps,
                    {"workload": "plain_lif_1k", "neurons": n, "sim_steps_per_step": cfg.steps,
-                    "block_steps": sim.block_steps, "tuned": tune["choice"]},
+                    "block_steps": sim.block_steps, "tuned": tune["choice"],
+                    "recorded": "raster of the LIF layer and V of neurons 0, 100, ..., 900 every step"},
                    neuron_steps_per_s=n * cfg.steps * args.steps / dev,
                    roofline={"bound": "hbm", "kernel": "k_update", "achieved": upd_bytes / upd / 1e9, "peak": peak,
                              "unit": "GB/s", "frac": upd_bytes / upd / 1e9 / peak, "peak_kind": kind,
                              "traffic": None},
+                   e2e={"value": ev / wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
+                        "d2h_bytes_per_step": int(8 * spikes / args.steps + 4 * len(trace_ids) * cfg.steps)},
                    gpu_launches=int(launches), clocks=clk)
 
 

@@ -69,3 +69,18 @@ def test_batch_rejects_ids_outside_their_instance():
     h = ctypes.c_void_p()
     st = lib.nbg_create_batch(ptrs, 2, ctypes.byref(opt), ctypes.byref(h), None)
     assert st != 0 and b"instance 0" in lib.nbg_last_error()
+
+
+def test_batch_rejects_instances_with_different_timesteps():
+    """Checked before any CUDA call."""
+    lib = _lib.load()
+    from neuronbridge_gb300.simulation import make_desc
+
+    a = _plastic_net(40, 1, 20.0)
+    made = [make_desc(a.flat(0.1)), make_desc(a.flat(0.2))]
+    ptrs = (ctypes.POINTER(_lib.NetDesc) * 2)(*[ctypes.pointer(m[0]) for m in made])
+    opt = _lib.Options()
+    lib.nbg_default_options(ctypes.byref(opt))
+    h = ctypes.c_void_p()
+    assert lib.nbg_create_batch(ptrs, 2, ctypes.byref(opt), ctypes.byref(h), None) != 0
+    assert b"share dt_ms" in lib.nbg_last_error()
