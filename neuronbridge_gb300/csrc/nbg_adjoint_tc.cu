@@ -81,6 +81,11 @@ __global__ void __launch_bounds__(256) k_lif_adj_split(
     __nv_bfloat16 *__restrict__ dI_hi, __nv_bfloat16 *__restrict__ dI_lo, float *__restrict__ g_theta,
     float *__restrict__ g_alpha, const float *__restrict__ alpha, const float *__restrict__ theta,
     nbg_lif_grad_params p, int N, int total) {
+    // programmatic dependent launch: the product that follows may start its
+    // prologue (and its W tiles) while this step runs; this step reads
+    // g_parts and lam_v only after the product before it has finished
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= total) return;
     const int j = idx % N;
@@ -148,10 +153,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    // Programmatic dependent launch: W does not change during the backward,
+    // so the first stages' W tiles are requested before the wait for the
+    // adjoint step that writes dI (a no-op without a programmatic launch).
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (warp == 0 && lane == 0) { // producer
-        for (int it = 0; it < iters; ++it) {
+        const int pre = iters < kAdjStages ? iters : kAdjStages;
+        for (int it = 0; it < pre; ++it) {
+            uint8_t *st = stages + it * kAdjStageBytes;
+            const size_t a_blk = (size_t)mt * kchunks + kc0 + it;
+            mbar_expect_tx(&full[it], kAdjStageBytes);
+            bulk_copy(st, (const uint8_t *)w_hi + a_blk * kAdjBlockA, kAdjBlockA, &full[it]);
+            bulk_copy(st + kAdjBlockA, (const uint8_t *)w_lo + a_blk * kAdjBlockA, kAdjBlockA, &full[it]);
+        }
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        for (int it = 0; it < pre; ++it) {
+            uint8_t *st = stages + it * kAdjStageBytes;
+            const int kc = kc0 + it;
+            bulk_copy(st + 2 * kAdjBlockA, (const uint8_t *)d_hi + (size_t)kc * kAdjBlockB, kAdjBlockB, &full[it]);
+            bulk_copy(st + 2 * kAdjBlockA + kAdjBlockB, (const uint8_t *)d_lo + (size_t)kc * kAdjBlockB, kAdjBlockB,
+                      &full[it]);
+        }
+        for (int it = pre; it < iters; ++it) {
             const int s = it % kAdjStages;
-            if (it >= kAdjStages && !mbar_wait(&empty[s], ((it / kAdjStages) & 1) ^ 1, abort)) break;
+            if (!mbar_wait(&empty[s], ((it / kAdjStages) & 1) ^ 1, abort)) break;
             uint8_t *st = stages + s * kAdjStageBytes;
             const int kc = kc0 + it;
             const size_t a_blk = (size_t)mt * kchunks + kc;
@@ -182,6 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         commit(done);
     }
     __syncwarp();
+    asm volatile("griddepcontrol.wait;" ::: "memory"); // the previous adjoint step has read g_parts
     // epilogue: warp w reads TMEM lanes 32*(w%4).. (rows i) and columns
     // 64*(w/4).. (batch rows b)
     mbar_wait(done, 0, abort);
@@ -383,9 +409,18 @@ nbg_status nbg_lif_adjoint_step_split(const float *g_parts, int n_parts, const f
         return nbg_fail(NBG_ERR_INVALID, "nbg_lif_adjoint_step_split: bad arguments (B must be %d, N a multiple of %d)",
                         kAdjN, kAdjM);
     const int total = B * N;
-    k_lif_adj_split<<<(total + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
-        g_parts, n_parts, g_read, c_t, u, s, m, vprev, lam_v, dI, (__nv_bfloat16 *)dI_hi, (__nv_bfloat16 *)dI_lo,
-        g_theta, g_alpha, alpha, theta, *p, N, total);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((total + 255) / 256);
+    cfg.blockDim = dim3(256);
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    NBG_CUDA(cudaLaunchKernelEx(&cfg, k_lif_adj_split, g_parts, n_parts, g_read, c_t, u, s, m, vprev, lam_v, dI,
+                                (__nv_bfloat16 *)dI_hi, (__nv_bfloat16 *)dI_lo, g_theta, g_alpha, alpha, theta, *p,
+                                N, total));
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }
@@ -401,9 +436,18 @@ nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *
         NBG_CUDA(cudaFuncSetAttribute(k_adj_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmemBytes));
         attr_set = true;
     }
-    k_adj_umma<<<dim3(N / kAdjM, split), kThreads, kAdjSmemBytes, (cudaStream_t)stream>>>(
-        (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo, (const __nv_bfloat16 *)dI_hi,
-        (const __nv_bfloat16 *)dI_lo, g_parts, N, split, err);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(N / kAdjM, split);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kAdjSmemBytes;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    NBG_CUDA(cudaLaunchKernelEx(&cfg, k_adj_umma, (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo,
+                                (const __nv_bfloat16 *)dI_hi, (const __nv_bfloat16 *)dI_lo, g_parts, N, split, err));
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

@@ -118,3 +118,40 @@ def test_reset_dense_subnetwork_matches_oracle(oracle_lib):
         assert np.array_equal(sim.state_field(f), o.state(f).astype(np.float32)), f
     assert sim.num_events == o.num_events
     assert sim.next_time == o.next_time == 551
+
+
+def test_input_layer_driving_a_dense_subnetwork(oracle_lib):
+    """Input-spike neurons stay in the main network (the reference's rule)
+    and drive a dense-tagged LIF layer: dense semantics chosen automatically,
+    external spikes delivered bit-exact against the oracle."""
+    rng = np.random.default_rng(21)
+    n_in, n = 32, 200
+    net = nb.Network()
+    net.add_layer(nb.NeuronLayer.input_spike(n_in))
+    net.add_layer(nb.NeuronLayer("TimeDrivenLIF_Voltage_jump", n, parameters={"dense_subnetwork_name": "core"}))
+    src = rng.integers(0, n_in, 3000).astype(np.int32)
+    tgt = rng.integers(n_in, n_in + n, 3000).astype(np.int32)
+    net.connect(nb.Connection(src, tgt, synapse_type=0, weight=rng.uniform(2.0, 6.0, 3000).astype(np.float32),
+                              delay=rng.integers(1, 6, 3000).astype(np.int32)))
+    rec_s = rng.integers(n_in, n_in + n, 2000).astype(np.int32)
+    rec_t = rng.integers(n_in, n_in + n, 2000).astype(np.int32)
+    net.connect(nb.Connection(rec_s, rec_t, synapse_type=(rng.random(2000) < 0.3).astype(np.int32), weight=1.5,
+                              delay=rng.integers(2, 9, 2000).astype(np.int32)))
+    cfg = nb.SimulationConfig(steps=400, timestep=0.1)
+    sim = nb.Simulation(net, cfg)
+    assert sim.semantics == "dense" and sim.dense_subnetwork_count == 1
+    _record_all(sim)
+    o = oracle_lib.OracleNet(net.to_native().flat(cfg.timestep, semantics=1))
+    pick = rng.choice(400 * n_in, 1500, replace=False)
+    t, i = pick // n_in, pick % n_in
+    sim.add_external_spikes(t, i)
+    o.add_external_spikes(t, i)
+    sim.run()
+    o.run(cfg.steps)
+    ts, is_ = _raw_raster(sim)
+    to, io = _oracle_spikes(o)
+    assert np.array_equal(ts, to) and np.array_equal(is_, io)
+    assert (is_ >= n_in).sum() > 0  # the dense layer fires
+    for f in range(5):
+        assert np.array_equal(sim.state_field(f), o.state(f).astype(np.float32)), f
+    assert sim.num_events == o.num_events
