@@ -56,6 +56,18 @@ nbg_status nbg_lif_forward_step_sparse(const float *xi, const float *w_rec, cons
                                        const nbg_lif_grad_params *p, int B, int N, void *stream);
 
 /* Ascending spike list of every row of the 0/1 matrix s (B x N). */
+/* L steps of nbg_lif_forward_step_sparse in one launch (rows are
+ * independent: each CTA runs its row through the L steps).  xi: L x B x N
+ * (x_t W_in of the L steps); spk/cnt: in, row b's ascending spike list of the
+ * step before the first, out, of the last step.  Optional outputs (NULL to
+ * skip), each L x B x N: s_out (s_t), u_rec, m_rec, vprev_rec; s_last (B x N,
+ * the last step's s); z += c[l] * s_t with c the L readout coefficients.
+ * Results are identical to L calls of nbg_lif_forward_step_sparse. */
+nbg_status nbg_lif_forward_segment_sparse(const float *xi, const float *w_rec, int32_t *spk, int32_t *cnt, float *v,
+                                          int32_t *ref, float *s_out, float *s_last, float *u_rec, uint8_t *m_rec,
+                                          float *vprev_rec, float *z, const float *c, const float *alpha,
+                                          const float *theta, const nbg_lif_grad_params *p, int L, int B, int N,
+                                          void *stream);
 nbg_status nbg_spike_lists(const float *s, int32_t *spk, int32_t *cnt, int B, int N, void *stream);
 
 /* One adjoint step (reverse time).  g_ext may be NULL (last step). */

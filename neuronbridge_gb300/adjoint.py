@@ -50,6 +50,8 @@ _SIG = {
     "nbg_lif_forward_step_sparse": (ctypes.c_int, [_vp] * 13 + [ctypes.c_float, _vp, _vp, ctypes.POINTER(GradParams),
                                                                 ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_spike_lists": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "nbg_lif_forward_segment_sparse": (ctypes.c_int, [_vp] * 15 + [ctypes.POINTER(GradParams), ctypes.c_int,
+                                                                  ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_adjoint_rec_prepare": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),
     "nbg_lif_adjoint_step_split": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_float] + [_vp] * 12 +
                                    [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp]),
@@ -108,6 +110,15 @@ class _SpikeLists:
     def load(self, lib, s, B, N, st):
         _lib.check(lib.nbg_spike_lists(_ptr(s), _ptr(self.idx[self.cur]), _ptr(self.cnt[self.cur]), B, N, st))
 
+    def segment(self, lib, xi, w_rec, v, ref, s_out, s_last, u_rec, m_rec, vp_rec, z, c, alpha, theta, p, L, B, N,
+                st):
+        """L steps in one launch (nbg_lif_forward_segment_sparse); the lists
+        are updated in place."""
+        _lib.check(lib.nbg_lif_forward_segment_sparse(
+            _ptr(xi), _ptr(w_rec), _ptr(self.idx[self.cur]), _ptr(self.cnt[self.cur]), _ptr(v), _ptr(ref),
+            _ptr(s_out), _ptr(s_last), _ptr(u_rec), _ptr(m_rec), _ptr(vp_rec), _ptr(z), _ptr(c), _ptr(alpha),
+            _ptr(theta), ctypes.byref(p), L, B, N, st))
+
     def step(self, lib, xi, w_rec, v, ref, s_out, u_rec, m_rec, vp_rec, z, c, alpha, theta, p, B, N, st):
         a, b = self.cur, self.cur ^ 1
         _lib.check(lib.nbg_lif_forward_step_sparse(
@@ -119,6 +130,20 @@ class _SpikeLists:
 
 def _sparse_ok(p, N: int) -> bool:
     return not p.smooth and N <= 2048
+
+
+_COEF = {}
+
+
+def _coef_device(coef, device) -> torch.Tensor:
+    """The readout coefficients on the device, made once per (values, device)
+    so that a CUDA graph capture finds them already there."""
+    key = (np.asarray(coef, np.float32).tobytes(), str(device))
+    t = _COEF.get(key)
+    if t is None:
+        t = torch.tensor(np.asarray(coef, np.float32), device=device)
+        _COEF[key] = t
+    return t
 
 
 # The recurrent product dI_{t+1} W_rec^T of the adjoint runs on the tensor
@@ -154,6 +179,7 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
     z.zero_()
     sparse = _sparse_ok(p, N)
     lists = _SpikeLists(B, N, x.device) if sparse else None  # no spikes before step 0
+    coef_dev = _coef_device(coef, x.device) if sparse else None
     I = torch.empty((B, N), device=x.device, dtype=torch.float32)
     for seg, t0 in enumerate(range(0, T, K)):
         t1 = min(T, t0 + K)
@@ -161,15 +187,16 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
         ck_ref[seg].copy_(ref)
         ck_s[seg].copy_(s_prev)
         xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
+        if sparse:  # the whole segment in one launch
+            s_prev = sbuf[seg & 1]
+            lists.segment(lib, xi, w_rec, v, ref, None, s_prev, None, None, None, z, coef_dev[t0:t1], alpha, theta,
+                          p, t1 - t0, B, N, st)
+            continue
         for t in range(t0, t1):
             s = sbuf[t & 1]
-            if sparse:
-                lists.step(lib, xi[t - t0], w_rec, v, ref, s, None, None, None, z, coef[t], alpha, theta, p, B, N, st)
-            else:
-                torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
-                _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
-                                                    float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N,
-                                                    st))
+            torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
+            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
+                                                float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
             s_prev = s
     torch.mm(z, w_out, out=out)
 
@@ -230,17 +257,15 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         v, ref = ck_v[seg].clone(), ck_ref[seg].clone()
         S[0].copy_(ck_s[seg])
         xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
-        if sparse:
+        if sparse:  # replay the segment in one launch, recording u, m, v_{t-1} and s
             lists.load(lib, S[0], B, N, st)
-        for k in range(L):
-            if sparse:
-                lists.step(lib, xi[k], w_rec, v, ref, S[k + 1], U[k], M[k], VP[k], None, 0.0, alpha, theta, p, B, N,
-                           st)
-                continue
-            torch.addmm(xi[k], S[k], w_rec, out=I)
-            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
-                                                _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
-                                                ctypes.byref(p), B, N, st))
+            lists.segment(lib, xi, w_rec, v, ref, S[1], None, U, M, VP, None, None, alpha, theta, p, L, B, N, st)
+        else:
+            for k in range(L):
+                torch.addmm(xi[k], S[k], w_rec, out=I)
+                _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
+                                                    _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
+                                                    ctypes.byref(p), B, N, st))
         for k in reversed(range(L)):
             t = t0 + k
             if tc:  # g_parts holds dI_{t+1} W_rec^T from the previous iteration

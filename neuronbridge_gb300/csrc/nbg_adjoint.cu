@@ -144,6 +144,121 @@ __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_sparse(
     if (tid == 0) cnt_out[b] = base;
 }
 
+// A whole checkpoint segment of the spike-driven forward: L steps of
+// k_lif_fwd_sparse in one launch.  Rows are independent (row b's input at
+// step t is x_t W_in plus the W_rec rows of row b's own spikes of step t-1),
+// so each CTA runs its row through all L steps with v and ref in registers
+// and the spike list in shared memory: no launch per step and no exchange
+// between CTAs.  The arithmetic is k_lif_fwd_sparse's, in the same order.
+__global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_segment(
+    const float *__restrict__ xi, const float *__restrict__ w, int *__restrict__ spk, int *__restrict__ cnt,
+    float *__restrict__ v, int *__restrict__ ref, float *__restrict__ s_out, float *__restrict__ s_last,
+    float *__restrict__ u_rec, unsigned char *__restrict__ m_rec, float *__restrict__ vprev_rec,
+    float *__restrict__ z, const float *__restrict__ c, const float *__restrict__ alpha,
+    const float *__restrict__ theta, nbg_lif_grad_params p, int L, int B, int N) {
+    extern __shared__ int seg_lists[]; // [2][N]
+    __shared__ int warp_base[kSparseThreads / 32 + 1];
+    __shared__ int list_cnt[2];
+    const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const size_t row = (size_t)b * N, plane = (size_t)B * N;
+    const int nq = (N + kSparseThreads - 1) / kSparseThreads;
+    float vv[kSparseCols], zz[kSparseCols];
+    int rr[kSparseCols];
+#pragma unroll
+    for (int q = 0; q < kSparseCols; ++q) {
+        const int j = tid + q * kSparseThreads;
+        vv[q] = zz[q] = 0.0f;
+        rr[q] = 0;
+        if (q < nq && j < N) {
+            vv[q] = v[row + j];
+            rr[q] = ref[row + j];
+            if (z) zz[q] = z[row + j];
+        }
+    }
+    if (tid == 0) list_cnt[0] = cnt[b];
+    __syncthreads();
+    for (int k = tid; k < list_cnt[0]; k += kSparseThreads) seg_lists[k] = spk[row + k];
+    __syncthreads();
+    int cur = 0;
+    for (int step = 0; step < L; ++step) {
+        const float *xs = xi + (size_t)step * plane + row;
+        float acc[kSparseCols];
+#pragma unroll
+        for (int q = 0; q < kSparseCols; ++q) {
+            const int j = tid + q * kSparseThreads;
+            acc[q] = (q < nq && j < N) ? xs[j] : 0.0f;
+        }
+        const int *list = seg_lists + cur * N;
+        const int nl = list_cnt[cur];
+        for (int k = 0; k < nl; ++k) {
+            const float *wr = w + (size_t)list[k] * N;
+#pragma unroll
+            for (int q = 0; q < kSparseCols; ++q) {
+                const int j = tid + q * kSparseThreads;
+                if (q < nq && j < N) acc[q] = acc[q] + __ldg(&wr[j]);
+            }
+        }
+        int *out_list = seg_lists + (cur ^ 1) * N;
+        int base = 0;
+        const float ct = z ? c[step] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < kSparseCols; ++q) {
+            if (q >= nq) break;
+            const int j = tid + q * kSparseThreads;
+            bool sp = false;
+            if (j < N) {
+                const size_t i = row + j, o = (size_t)step * plane + i;
+                const float vp = vv[q];
+                const int rf = rr[q];
+                const bool m = rf == 0;
+                const float u = m ? vp + alpha[j] * (p.v_rest - vp) + acc[q] : p.v_reset;
+                const float sv = u > theta[j] ? 1.0f : 0.0f;
+                vv[q] = u - sv * (u - p.v_reset);
+                rr[q] = sv > 0.0f ? p.t_ref : (rf > 0 ? rf - 1 : 0);
+                if (s_out) s_out[o] = sv;
+                if (s_last && step == L - 1) s_last[i] = sv;
+                if (u_rec) u_rec[o] = u;
+                if (m_rec) m_rec[o] = m ? 1 : 0;
+                if (vprev_rec) vprev_rec[o] = vp;
+                if (z) zz[q] = zz[q] + ct * sv;
+                sp = sv > 0.0f;
+            }
+            // ordered compaction of this chunk's spikes into the next list
+            const unsigned bal = __ballot_sync(0xffffffffu, sp);
+            if (lane == 0) warp_base[wid] = __popc(bal);
+            __syncthreads();
+            if (tid == 0) {
+                int sum = 0;
+                for (int k = 0; k < kSparseThreads / 32; ++k) {
+                    const int cc = warp_base[k];
+                    warp_base[k] = sum;
+                    sum += cc;
+                }
+                warp_base[kSparseThreads / 32] = sum;
+            }
+            __syncthreads();
+            if (sp) out_list[base + warp_base[wid] + __popc(bal & ((1u << lane) - 1u))] = j;
+            base += warp_base[kSparseThreads / 32];
+            __syncthreads();
+        }
+        if (tid == 0) list_cnt[cur ^ 1] = base;
+        __syncthreads();
+        cur ^= 1;
+    }
+#pragma unroll
+    for (int q = 0; q < kSparseCols; ++q) {
+        const int j = tid + q * kSparseThreads;
+        if (q < nq && j < N) {
+            v[row + j] = vv[q];
+            ref[row + j] = rr[q];
+            if (z) z[row + j] = zz[q];
+        }
+    }
+    const int nl = list_cnt[cur];
+    for (int k = tid; k < nl; k += kSparseThreads) spk[row + k] = seg_lists[cur * N + k];
+    if (tid == 0) cnt[b] = nl;
+}
+
 // Ascending spike list of each row of a 0/1 matrix (segment restarts).
 __global__ void __launch_bounds__(kSparseThreads) k_spike_list(const float *__restrict__ s, int *__restrict__ idx,
                                                                int *__restrict__ cnt, int N) {
@@ -233,6 +348,24 @@ nbg_status nbg_lif_forward_step_sparse(const float *xi, const float *w_rec, cons
     k_lif_fwd_sparse<<<B, kSparseThreads, 0, (cudaStream_t)stream>>>(xi, w_rec, spk_in, cnt_in, spk_out, cnt_out, v,
                                                                       ref, s_out, u_rec, m_rec, vprev_rec, z, c_t,
                                                                       alpha, theta, *p, N);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_lif_forward_segment_sparse(const float *xi, const float *w_rec, int32_t *spk, int32_t *cnt, float *v,
+                                          int32_t *ref, float *s_out, float *s_last, float *u_rec, uint8_t *m_rec,
+                                          float *vprev_rec, float *z, const float *c, const float *alpha,
+                                          const float *theta, const nbg_lif_grad_params *p, int L, int B, int N,
+                                          void *stream) {
+    if (!xi || !w_rec || !spk || !cnt || !v || !ref || !alpha || !theta || !p || (z && !c) || L <= 0 || B <= 0 ||
+        N <= 0)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_forward_segment_sparse: bad arguments");
+    if (p->smooth) return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step needs binary spikes (smooth = 0)");
+    if (N > kSparseThreads * kSparseCols)
+        return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step supports up to %d neurons",
+                        kSparseThreads * kSparseCols);
+    k_lif_fwd_segment<<<B, kSparseThreads, 2 * N * sizeof(int), (cudaStream_t)stream>>>(
+        xi, w_rec, spk, cnt, v, ref, s_out, s_last, u_rec, m_rec, vprev_rec, z, c, alpha, theta, *p, L, B, N);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

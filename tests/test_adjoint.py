@@ -193,3 +193,48 @@ def test_tensor_core_recurrent_product(monkeypatch):
         scale = r.grad.abs().max().item()
         assert (g.double().cpu() - r.grad).abs().max().item() <= 1e-3 * scale, name
         assert (g - h).abs().max().item() <= 1e-3 * h.abs().max().item(), name
+
+
+@pytest.mark.gpu
+def test_segment_forward_equals_per_step_launches():
+    """nbg_lif_forward_segment_sparse (a checkpoint segment in one launch, each
+    CTA running its row through every step) gives bit for bit what one
+    nbg_lif_forward_step_sparse launch per step gives."""
+    from neuronbridge_gb300.adjoint import GradParams, _bind, _SpikeLists, _stream
+
+    lib = _bind()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    B, N, L = 48, 640, 37
+    w = torch.randn(N, N, device="cuda", generator=g) * 0.3
+    xi = torch.rand(L, B, N, device="cuda", generator=g) * 0.3
+    alpha = torch.full((N,), 0.05, device="cuda")
+    theta = torch.rand(N, device="cuda", generator=g) * 0.5 + 0.5
+    p = GradParams(0.0, 0.0, 10.0, 3, 0)
+    c = torch.linspace(0.1, 1.0, L, device="cuda")
+    s0 = (torch.rand(B, N, device="cuda", generator=g) < 0.05).float()
+    v0 = torch.rand(B, N, device="cuda", generator=g)
+    ref0 = torch.randint(0, 4, (B, N), device="cuda", dtype=torch.int32, generator=g)
+    st = _stream()
+    out = []
+    for segment in (False, True):
+        lists = _SpikeLists(B, N, "cuda")
+        v, ref = v0.clone(), ref0.clone()
+        S = torch.zeros((L + 1, B, N), device="cuda")
+        U = torch.zeros((L, B, N), device="cuda")
+        M = torch.zeros((L, B, N), device="cuda", dtype=torch.uint8)
+        VP = torch.zeros((L, B, N), device="cuda")
+        z = torch.zeros((B, N), device="cuda")
+        lists.load(lib, s0, B, N, st)
+        if segment:
+            lists.segment(lib, xi, w, v, ref, S[1], None, U, M, VP, z, c, alpha, theta, p, L, B, N, st)
+        else:
+            for k in range(L):
+                lists.step(lib, xi[k], w, v, ref, S[k + 1], U[k], M[k], VP[k], z, float(c[k]), alpha, theta, p, B,
+                           N, st)
+        torch.cuda.synchronize()
+        cnt = lists.cnt[lists.cur].clone()
+        idx = torch.cat([lists.idx[lists.cur][b][:int(cnt[b])] for b in range(B)])
+        out.append((v, ref, S, U, M, VP, z, cnt, idx))
+    assert out[0][2].sum() > 0  # the rows spike
+    for a, b in zip(out[0], out[1]):
+        assert torch.equal(a, b)
