@@ -965,6 +965,8 @@ struct nbg_engine {
     std::vector<nbg_stdp_desc> rules;
     std::vector<float> init_v, init_u, init_iext;
     std::vector<int> woff_host; // first mask word of each neuron (N + 1 entries)
+    int *pin_ids = nullptr, *pin_t = nullptr; // pinned staging of the raster download
+    size_t pin_cap = 0;
     std::vector<float> init_w;
     // device buffers
     DevBuf<unsigned short> pop;
@@ -1294,9 +1296,9 @@ class Barrier {
 // the ids of each step are sorted.  A counting sort by step (per-thread
 // histograms over contiguous chunks, one prefix pass, a scatter) and the
 // per-step sorts run on up to 16 host threads for large rasters.
-void assemble_raster(nbg_engine *e, const std::vector<int> &ts, const std::vector<int> &ids,
+void assemble_raster(nbg_engine *e, const int *ts, const int *ids, size_t n,
                      const std::vector<std::pair<int, int>> &ext, int t0, int count) {
-    const size_t n = ids.size(), steps = (size_t)count;
+    const size_t steps = (size_t)count;
     const size_t total = n + ext.size();
     const size_t base = e->spk_id.size();
     e->spk_id.resize(base + total);
@@ -1820,6 +1822,8 @@ nbg_status nbg_destroy(nbg_engine *e) {
     for (auto ev : e->tev)
         if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->pin_ids) cudaFreeHost(e->pin_ids);
+    if (e->pin_t) cudaFreeHost(e->pin_t);
     delete e;
     return NBG_OK;
 }
@@ -2038,16 +2042,26 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     // spikes of output neurons, bucketed by step and sorted by id within it
     unsigned int ndev = 0;
     NBG_CUDA(cudaMemcpy(&ndev, e->cursor.p, sizeof(ndev), cudaMemcpyDeviceToHost));
-    std::vector<int> ids((size_t)ndev), ts((size_t)ndev);
+    // downloaded into pinned staging buffers (grown by half again when short)
+    if ((size_t)ndev > e->pin_cap) {
+        if (e->pin_ids) cudaFreeHost(e->pin_ids);
+        if (e->pin_t) cudaFreeHost(e->pin_t);
+        e->pin_ids = e->pin_t = nullptr;
+        e->pin_cap = 0;
+        const size_t cap = (size_t)ndev + (size_t)ndev / 2;
+        NBG_CUDA(cudaMallocHost(&e->pin_ids, cap * sizeof(int)));
+        NBG_CUDA(cudaMallocHost(&e->pin_t, cap * sizeof(int)));
+        e->pin_cap = cap;
+    }
     if (ndev > 0) {
-        NBG_CUDA(cudaMemcpy(ids.data(), e->out_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
-        NBG_CUDA(cudaMemcpy(ts.data(), e->out_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(e->pin_ids, e->out_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(e->pin_t, e->out_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
     }
     {
         std::vector<std::pair<int, int>> ext_rec; // external spikes of recorded neurons
         for (const auto &x : ext_due)
             if (e->layers[e->pop_host[x.second]].record) ext_rec.push_back(x);
-        assemble_raster(e, ts, ids, ext_rec, t0, count);
+        assemble_raster(e, e->pin_t, e->pin_ids, (size_t)ndev, ext_rec, t0, count);
     }
     if (ntr > 0) {
         const size_t rb = e->trace_rows.size();
