@@ -84,3 +84,8 @@ def test_batch_rejects_instances_with_different_timesteps():
     h = ctypes.c_void_p()
     assert lib.nbg_create_batch(ptrs, 2, ctypes.byref(opt), ctypes.byref(h), None) != 0
     assert b"share dt_ms" in lib.nbg_last_error()
+
+
+def test_batch_rejects_an_empty_list():
+    with pytest.raises(TypeError):
+        nb.Simulation.batch([], nb.SimulationConfig(steps=10, timestep=0.1))

@@ -105,6 +105,9 @@ def test_reset_dense_subnetwork_matches_oracle(oracle_lib):
     o = oracle_lib.OracleNet(net.to_native().flat(cfg.timestep, semantics=1))
     sim.run(250)
     o.run(250)
+    assert sim.lib.nbg_reset_neurons(sim._h, -1, 5) != 0  # range outside the network
+    assert sim.lib.nbg_reset_neurons(sim._h, 490, 20) != 0
+    assert sim.lib.nbg_reset_neurons(sim._h, 10, 0) == 0  # empty range: nothing to do
     sim.reset_dense_subnetwork("core")
     o.reset_neurons(200, 300)
     for f in range(5):
