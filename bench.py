@@ -26,9 +26,11 @@ With --impl reference the CPU oracle port (oracle/, a restatement of the
 reference's CPU path; the reference itself does not build here) is timed on a
 bounded sample of the same workload on the host cores.
 
-N > 1 (torchrun): the network does not shard, so every rank runs an
+N > 1 (torchrun): the headline network does not shard, so every rank runs an
 independent replica; `value` sums the events of all ranks over the slowest
-rank's time.
+rank's time.  The batched workload shards its instances over the ranks
+(greedy size-balanced bin packing, neuronbridge_gb300/partition.py) and
+reports strong scaling; lif, dense and adjoint run on rank 0 alone.
 """
 from __future__ import annotations
 
@@ -259,43 +261,72 @@ def bench_lif(args) -> dict:
                    gpu_launches=int(launches), clocks=clk)
 
 
-def bench_batched(args) -> dict:
+def bench_batched(args) -> dict | None:
     """256 LIF instances (500..50,000 neurons each): one engine over the
     union, autotuned launch shape, one graph per run(1,000) call, against the
-    same 256 networks each in its own engine, run one after the other."""
-    import neuronbridge_gb300 as nb
-    from neuronbridge_gb300 import tuning, workloads
+    same 256 networks each in its own engine, run one after the other.
 
+    Under torchrun the instances shard over the ranks by greedy size-balanced
+    bin packing (every rank builds one batched engine over its share; no
+    data-path collective): the total work is fixed, so the scaling is strong.
+    `value` sums the events of all ranks over the slowest rank's device time."""
+    import torch
+
+    import neuronbridge_gb300 as nb
+    from neuronbridge_gb300 import workloads
+    from neuronbridge_gb300.partition import partition_instances, shard_loads
+    from neuronbridge_gb300.replicas import aggregate
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    sizes, _ = workloads.batched_params(args.instances)
+    shards = partition_instances(sizes, world)
+    mine = shards[rank]
     t0 = time.perf_counter()
-    singles, union, cfg = workloads.batched_lif(instances=args.instances)
+    singles = [workloads.batched_instance(int(k), args.instances) for k in mine]
     build_s = time.perf_counter() - t0
-    sim = nb.Simulation.batch(singles, cfg)  # one engine over the 256 instances (nbg_create_batch)
-    tune = _launch_shape(sim, args, 300)
-    for _ in range(args.warmup):
-        sim.run(cfg.steps)
-        sim.clear_spikes()
+    cfg = nb.SimulationConfig(steps=1000, timestep=0.1)
+    n_lif = int(sizes[mine].sum())
     ev = dev = wall = 0.0
     launches = 0
-    clocks = ClockSampler(0)
-    clocks.start()
-    for _ in range(args.steps):
-        e0 = sim.num_events
-        w0 = time.perf_counter()
-        sim.run(cfg.steps)
-        wall += time.perf_counter() - w0
-        p = sim.bench_profiling_snapshot()
-        ev += sim.num_events - e0
-        dev += p["device_ms"] / 1e3
-        launches += p["kernel_launches"]
-        sim.clear_spikes()
-    clk = clocks.stop()
-    n_lif = union.neuron_count // 2
-    block_steps = sim.block_steps
-    del sim
+    tune = {"choice": None}
+    block_steps = None
+    clk = None
+    if len(mine):
+        sim = nb.Simulation.batch(singles, cfg, device=local)  # one engine over the shard (nbg_create_batch)
+        tune = _launch_shape(sim, args, 300)
+        for _ in range(args.warmup):
+            sim.run(cfg.steps)
+            sim.clear_spikes()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    if len(mine):
+        clocks = ClockSampler(local)
+        clocks.start()
+        for _ in range(args.steps):
+            e0 = sim.num_events
+            w0 = time.perf_counter()
+            sim.run(cfg.steps)
+            wall += time.perf_counter() - w0
+            p = sim.bench_profiling_snapshot()
+            ev += sim.num_events - e0
+            dev += p["device_ms"] / 1e3
+            launches += p["kernel_launches"]
+            sim.clear_spikes()
+        clk = clocks.stop()
+        block_steps = sim.block_steps
+        del sim
+    torch.cuda.synchronize()
     # plain form: every instance in its own engine, one after another
     p_ev = p_dev = p_wall = 0.0
     for net in singles:
-        s = nb.Simulation(net, cfg)
+        s = nb.Simulation(net, cfg, device=local)
         s.run(cfg.steps)  # warm (first call: steps + 1 updates)
         e0 = s.num_events
         w0 = time.perf_counter()
@@ -304,32 +335,49 @@ def bench_batched(args) -> dict:
         p_ev += s.num_events - e0
         p_dev += s.bench_profiling_snapshot()["device_ms"] / 1e3
         s.close()
-    value = ev / dev
-    plain = p_ev / p_dev
+    dev_dev = f"cuda:{local}" if world > 1 else None
+    (dev_all, wall_all, p_dev_all, p_wall_all), (ev_all, p_ev_all) = aggregate(
+        [dev, wall, p_dev, p_wall], [ev, p_ev], device=dev_dev)
+    if rank != 0:
+        return None
+    value = ev_all / dev_all
+    plain = p_ev_all / p_dev_all
     # the Poisson layers have no inputs: the engine evaluates them inline at
-    # their targets, so the neuron-steps are the LIF neurons'
+    # their targets, so the neuron-steps are the LIF neurons' (rank 0's share
+    # for the kernel roofline)
     upd_bytes = BYTES_PER_LIF_NEURON_STEP * n_lif * cfg.steps * args.steps + BYTES_PER_STATIC_EVENT * ev
     peak, kind = _peaks()
     per_launch = launches / args.steps
-    return _common(args, "synaptic events/s", value, "synaptic events/s", 1e3 * dev / args.steps,
-                   {"workload": f"batched_lif_{args.instances}", "instances": args.instances, "lif_neurons": n_lif,
-                    "sim_steps_per_step": cfg.steps, "block_steps": block_steps, "tuned": tune["choice"],
-                    "host_build_s": build_s},
-                   neuron_steps_per_s=n_lif * cfg.steps * args.steps / dev,
-                   roofline={"bound": "hbm", "kernel": "k_update<Spec<1, 0>> (LIF, static; Poisson generators packed "
-                                                       "eight per thread)",
+    loads = shard_loads(sizes, shards)
+    config = {"workload": f"batched_lif_{args.instances}", "instances": args.instances,
+              "lif_neurons": int(sizes.sum()), "sim_steps_per_step": cfg.steps, "block_steps": block_steps,
+              "tuned": tune["choice"], "host_build_s": build_s,
+              "l2": "inputs larger than L2 (2.2 GB of synapse columns per launch)",
+              "parallelism": "single" if world == 1 else
+              f"instances sharded over {world} ranks (greedy size-balanced bin packing)"}
+    if world > 1:
+        config["shard_instances"] = [int(len(s)) for s in shards]
+        config["shard_lif_neurons"] = [int(x) for x in loads]
+    line = _common(args, "synaptic events/s", value, "synaptic events/s", 1e3 * dev_all / args.steps, config,
+                   neuron_steps_per_s=int(sizes.sum()) * cfg.steps * args.steps / dev_all,
+                   roofline={"bound": "hbm", "kernel": "k_update<Spec<1, 0>> (LIF, static; Poisson generators "
+                                                       "packed eight per thread)",
                              "achieved": upd_bytes / dev / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": upd_bytes / dev / 1e9 / peak, "peak_kind": kind,
-                             "traffic": (BATCHED_TRAFFIC_BYTES if args.instances == 256 else None),
+                             "traffic": (BATCHED_TRAFFIC_BYTES if args.instances == 256 and world == 1 else None),
                              "traffic_unit": "bytes per launch (ncu on 32 instances, scaled by units)",
                              "algorithmic_bytes_per_launch": upd_bytes / (per_launch * args.steps),
                              "avg_update_launch_us": 1e6 * dev / launches if launches else None},
-                   plain={"value": plain, "unit": "synaptic events/s", "device_s_per_1000_steps": p_dev,
-                          "wall_s_per_1000_steps": p_wall},
+                   plain={"value": plain, "unit": "synaptic events/s", "device_s_per_1000_steps": p_dev_all,
+                          "wall_s_per_1000_steps": p_wall_all},
                    speedup_vs_plain=value / plain,
-                   e2e={"value": ev / wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
+                   e2e={"value": ev_all / wall_all, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
                         "d2h_bytes_per_step": None},
                    gpu_launches=int(launches), clocks=clk)
+    line["n_gpus"] = world
+    if world > 1:
+        line["scaling"] = "strong"
+    return line
 
 
 def bench_dense(args) -> dict:
@@ -453,7 +501,14 @@ def main() -> None:
         run_reference(args)
         return
     if args.workload != "izh":
-        fn = {"lif": bench_lif, "batched": bench_batched, "dense": bench_dense, "adjoint": bench_adjoint}
+        if args.workload == "batched":
+            line = bench_batched(args)
+            if line is not None:
+                print(json.dumps(line), flush=True)
+            return
+        if _dist()[1] != 0:
+            return  # lif, dense and adjoint measure one GPU: rank 0 alone runs them
+        fn = {"lif": bench_lif, "dense": bench_dense, "adjoint": bench_adjoint}
         print(json.dumps(fn[args.workload](args)), flush=True)
         return
 
