@@ -241,7 +241,7 @@ def bench_lif(args) -> dict:
         ev += sim.num_events - e0
         dev += p["device_ms"] / 1e3
         upd += p["device_ms"] / 1e3
-        launches += p["kernel_launches"]
+        launches += p["kernel_launches"] + p["raster_order_launches"]
         sim.clear_spikes()
         flush.fill_(1.0)
     clk = clocks.stop()
@@ -294,6 +294,7 @@ def bench_batched(args) -> dict | None:
     n_lif = int(sizes[mine].sum())
     ev = dev = wall = 0.0
     launches = 0
+    raster = {"order_ms": 0.0, "download_ms": 0.0, "append_ms": 0.0, "order_launches": 0}
     tune = {"choice": None}
     block_steps = None
     clk = None
@@ -318,6 +319,8 @@ def bench_batched(args) -> dict | None:
             ev += sim.num_events - e0
             dev += p["device_ms"] / 1e3
             launches += p["kernel_launches"]
+            for k in raster:
+                raster[k] += p["raster_" + k]
             sim.clear_spikes()
         clk = clocks.stop()
         block_steps = sim.block_steps
@@ -373,7 +376,8 @@ def bench_batched(args) -> dict | None:
                    speedup_vs_plain=value / plain,
                    e2e={"value": ev_all / wall_all, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
                         "d2h_bytes_per_step": None},
-                   gpu_launches=int(launches), clocks=clk)
+                   raster_per_run_call={k: v / max(1, args.steps) for k, v in raster.items()},
+                   gpu_launches=int(launches + raster["order_launches"]), clocks=clk)
     line["n_gpus"] = world
     if world > 1:
         line["scaling"] = "strong"
@@ -547,6 +551,8 @@ def main() -> None:
         sim.clear_spikes()
         return ev, wall, prof, ids, len(ids)
 
+    raster = {"order_ms": 0.0, "download_ms": 0.0, "append_ms": 0.0, "order_launches": 0}
+
     for _ in range(args.warmup):
         bench_step()
         flush.fill_(1.0)
@@ -567,6 +573,8 @@ def main() -> None:
         tot_spk += nspk
         tot_post += int(fan[new_ids].sum())
         launches += prof["kernel_launches"]
+        for k in raster:
+            raster[k] += prof["raster_" + k]
         flush.fill_(1.0)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -608,7 +616,8 @@ def main() -> None:
                      "avg_update_launch_us": 1e6 * tot_upd / max(1, launches)},
         "e2e": {"value": tot_ev_all / tot_wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 4 + 8 + 4,
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": int(launches),
+        "raster_per_run_call": {k: v / args.steps for k, v in raster.items()},
+        "gpu_launches": int(launches + raster["order_launches"]),
         "clocks": clk,
     }
     if not args.no_cpu_baseline:

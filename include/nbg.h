@@ -286,6 +286,15 @@ nbg_status nbg_get_logged_events(nbg_engine *e, int32_t *t, int64_t *conn, float
 nbg_status nbg_profile(nbg_engine *e, double *total_ms, double *update_ms, double *propagate_ms,
                        int64_t *launches);
 
+/* Raster phases of the last nbg_run call: the device ordering of its spike
+ * raster into (step, id) order (CUDA events; order_launches kernels), the
+ * download to the host and the append to the recorded raster (host wall
+ * time).  The reference records output spikes from its host event loop
+ * (communication/src/ArrayOutputSpikeDriver.cpp); here they are this
+ * separate phase after the step loop. */
+nbg_status nbg_raster_profile(nbg_engine *e, double *order_ms, double *download_ms, double *append_ms,
+                              int64_t *order_launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -113,6 +113,7 @@ _SIGNATURES = {
     "nbg_num_logged_events": (ctypes.c_int, [ctypes.c_void_p, _i64p]),
     "nbg_get_logged_events": (ctypes.c_int, [ctypes.c_void_p, _i32p, _i64p, _f32p]),
     "nbg_profile": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p, _i64p]),
+    "nbg_raster_profile": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p, _i64p]),
 }
 
 

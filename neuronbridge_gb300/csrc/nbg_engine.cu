@@ -43,11 +43,14 @@
 
 #include <algorithm>
 #include <cmath>
-#include <condition_variable>
-#include <mutex>
+#include <chrono>
+#include <memory>
 #include <thread>
+#include <type_traits>
+#include <utility>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -941,6 +944,25 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
 
 NBG_HIDDEN cudaError_t nbg_device_decay_table(float *tab, const float *inv_host, int rows, int len, float dt);
 
+// Largest spike bitmap of the raster ordering, in 32-bit words (1 GiB); the
+// environment variable NBG_RASTER_BITMAP_WORDS overrides it at creation.
+constexpr size_t kRasterBitmapWords = (size_t)1 << 28;
+
+// Allocator whose value-initialisation leaves trivially constructible
+// elements uninitialised: the raster vectors grow by up to hundreds of MB per
+// run call and are overwritten right after.
+template <class T> struct NoInitAlloc : std::allocator<T> {
+    template <class U> struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U> NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+    template <class U> void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+        ::new ((void *)p) U;
+    }
+    template <class U, class... A> void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+
 struct nbg_engine {
     int device = 0;
     int N = 0;
@@ -967,6 +989,15 @@ struct nbg_engine {
     std::vector<int> woff_host; // first mask word of each neuron (N + 1 entries)
     int *pin_ids = nullptr, *pin_t = nullptr; // pinned staging of the raster download
     size_t pin_cap = 0;
+    int sm_count = 1;
+    size_t raster_bitmap_words = kRasterBitmapWords;
+    // raster ordering: per-step spike bitmap, tile sums / positions, running
+    // base, ordered entries; timings of the last run call's raster phases
+    DevBuf<unsigned int> rbm, rtile, rbase;
+    DevBuf<int> ord_ids, ord_t;
+    cudaEvent_t evr0 = nullptr, evr1 = nullptr;
+    double last_order_ms = 0.0, last_download_ms = 0.0, last_append_ms = 0.0;
+    int64_t last_order_launches = 0;
     std::vector<float> init_w;
     // device buffers
     DevBuf<unsigned short> pop;
@@ -987,7 +1018,7 @@ struct nbg_engine {
     // time / recording
     int next_t = 0;
     bool ran = false;
-    std::vector<int32_t> spk_t, spk_id;
+    std::vector<int32_t, NoInitAlloc<int32_t>> spk_t, spk_id; // growth does not zero-fill
     std::vector<int32_t> trace_ids;
     std::vector<float> trace_rows;
     int64_t trace_nrows = 0;
@@ -1267,89 +1298,226 @@ nbg_status harvest_timing(nbg_engine *e, int blocks) {
     return NBG_OK;
 }
 
-// Reusable barrier for the raster assembly threads.
-class Barrier {
-  public:
-    explicit Barrier(int n) : n_(n) {}
-    void wait() {
-        std::unique_lock<std::mutex> lk(m_);
-        const unsigned long long gen = gen_;
-        if (++arrived_ == n_) {
-            arrived_ = 0;
-            ++gen_;
-            cv_.notify_all();
-        } else {
-            cv_.wait(lk, [&] { return gen_ != gen; });
+// ---------------------------------------------------------------------------
+// Raster ordering on the device.  The update kernel appends (step, id)
+// entries in warp order; a run call returns its raster in (step, id) order.
+// A spike bitmap per step gives that order without a sort: every entry sets
+// its bit, a popcount scan over the bitmap words gives each word its first
+// output position, and the set bits are written out word by word.  A neuron
+// spikes at most once per step, so the bitmap holds every entry (the host
+// checks that the emitted count equals the entry count).  Bitmap rows are
+// padded to whole 16-byte groups and the bitmap to whole tiles; long calls
+// are ordered in chunks of steps whose bitmap fits the budget.
+constexpr int kRasterThreads = 256;
+constexpr int kRasterWordsPerThread = 16;                                  // four 16-byte loads
+constexpr int kRasterTileWords = kRasterThreads * kRasterWordsPerThread;  // words per CTA
+constexpr int kRasterScanThreads = 1024, kRasterScanPerThread = 8;
+
+// Exclusive prefix sum over the block of x (blockDim.x a multiple of 32, at
+// most 1024); *total receives the block's sum.  wt: 33 words of shared memory.
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned x, unsigned *wt, unsigned *total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wt[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const unsigned v = lane < nw ? wt[lane] : 0u;
+        unsigned vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, vi, o);
+            if (lane >= o) vi += y;
+        }
+        if (lane < nw) wt[lane] = vi - v;
+        if (lane == 31) wt[32] = vi;
+    }
+    __syncthreads();
+    *total = wt[32];
+    return wt[wid] + inc - x;
+}
+
+__global__ void k_raster_mark(const int *__restrict__ ts, const int *__restrict__ ids, unsigned n, int t_lo,
+                              int steps, int wp, int n_neurons, unsigned *__restrict__ bm) {
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int s = ts[i] - t_lo;
+        const int id = ids[i];
+        if (s < 0 || s >= steps || id < 0 || id >= n_neurons) continue;
+        atomicOr(bm + (size_t)s * (size_t)wp + (size_t)(id >> 5), 1u << (id & 31));
+    }
+}
+
+__global__ void __launch_bounds__(kRasterThreads) k_raster_count(const uint4 *__restrict__ bm,
+                                                                 unsigned *__restrict__ tile_sum) {
+    __shared__ unsigned wt[33];
+    const uint4 *q = bm + ((size_t)blockIdx.x * kRasterTileWords + (size_t)threadIdx.x * kRasterWordsPerThread) / 4;
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < kRasterWordsPerThread / 4; ++k) {
+        const uint4 v = q[k];
+        c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+    }
+    unsigned total;
+    block_exclusive_scan(c, wt, &total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// One CTA: tile sums -> first output position of each tile, continuing from
+// *base (the entries of earlier chunks); *base advances by the chunk's total.
+__global__ void __launch_bounds__(kRasterScanThreads) k_raster_scan(unsigned *__restrict__ tile, unsigned n_tiles,
+                                                                    unsigned *__restrict__ base) {
+    __shared__ unsigned wt[33];
+    unsigned carry = *base;
+    __syncthreads();
+    for (unsigned c0 = 0; c0 < n_tiles; c0 += kRasterScanThreads * kRasterScanPerThread) {
+        const unsigned i0 = c0 + threadIdx.x * kRasterScanPerThread;
+        unsigned v[kRasterScanPerThread], sum = 0;
+#pragma unroll
+        for (int k = 0; k < kRasterScanPerThread; ++k) {
+            v[k] = i0 + k < n_tiles ? tile[i0 + k] : 0u;
+            sum += v[k];
+        }
+        unsigned total;
+        unsigned run = carry + block_exclusive_scan(sum, wt, &total);
+#pragma unroll
+        for (int k = 0; k < kRasterScanPerThread; ++k) {
+            if (i0 + k < n_tiles) tile[i0 + k] = run;
+            run += v[k];
+        }
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *base = carry;
+}
+
+__global__ void __launch_bounds__(kRasterThreads) k_raster_emit(const uint4 *__restrict__ bm,
+                                                                const unsigned *__restrict__ tile_pos, int wp,
+                                                                int t_lo, int *__restrict__ out_ids,
+                                                                int *__restrict__ out_t) {
+    __shared__ unsigned wt[33];
+    const size_t w0 = (size_t)blockIdx.x * kRasterTileWords + (size_t)threadIdx.x * kRasterWordsPerThread;
+    const uint4 *q = bm + w0 / 4;
+    unsigned w[kRasterWordsPerThread], c = 0;
+#pragma unroll
+    for (int k = 0; k < kRasterWordsPerThread / 4; ++k) {
+        const uint4 v = q[k];
+        w[4 * k + 0] = v.x;
+        w[4 * k + 1] = v.y;
+        w[4 * k + 2] = v.z;
+        w[4 * k + 3] = v.w;
+        c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+    }
+    unsigned total;
+    unsigned pos = tile_pos[blockIdx.x] + block_exclusive_scan(c, wt, &total);
+    if (c == 0) return;
+    size_t s = w0 / (size_t)wp;
+    int col = (int)(w0 - s * (size_t)wp);
+#pragma unroll
+    for (int k = 0; k < kRasterWordsPerThread; ++k) {
+        unsigned m = w[k];
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            out_ids[pos] = (col << 5) + b;
+            out_t[pos] = t_lo + (int)s;
+            ++pos;
+        }
+        if (++col == wp) {
+            col = 0;
+            ++s;
         }
     }
+}
 
-  private:
-    std::mutex m_;
-    std::condition_variable cv_;
-    int n_, arrived_ = 0;
-    unsigned long long gen_ = 0;
-};
-
-// Append one run call's raster to spk_t / spk_id in (step, id) order.  The
-// device entries (ts, ids) come in warp order; ext holds the external spikes
-// of recorded neurons, which follow the device entries of their step before
-// the ids of each step are sorted.  A counting sort by step (per-thread
-// histograms over contiguous chunks, one prefix pass, a scatter) and the
-// per-step sorts run on up to 16 host threads for large rasters.
-void assemble_raster(nbg_engine *e, const int *ts, const int *ids, size_t n,
-                     const std::vector<std::pair<int, int>> &ext, int t0, int count) {
-    const size_t steps = (size_t)count;
-    const size_t total = n + ext.size();
-    const size_t base = e->spk_id.size();
-    e->spk_id.resize(base + total);
-    e->spk_t.resize(base + total);
-    int *out_id = e->spk_id.data() + base, *out_t = e->spk_t.data() + base;
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int T = n >= ((size_t)1 << 16) ? (int)std::min(16u, hw) : 1;
-    std::vector<size_t> hist((size_t)T * steps, 0); // thread k, step s: count, then write position
-    std::vector<size_t> at(steps + 1, 0);           // first position of each step
-    auto chunk_begin = [&](int k) { return n * (size_t)k / (size_t)T; };
-    auto body = [&](int k, Barrier *bar) {
-        size_t *h = hist.data() + (size_t)k * steps;
-        for (size_t i = chunk_begin(k); i < chunk_begin(k + 1); ++i) ++h[(size_t)(ts[i] - t0)];
-        if (bar) bar->wait();
-        if (k == 0) { // write positions: step by step, thread chunks in order, then external spikes
-            std::vector<size_t> ext_cnt(steps, 0), next_ext(steps, 0);
-            for (const auto &x : ext) ++ext_cnt[(size_t)(x.first - t0)];
-            size_t pos = 0;
-            for (size_t st = 0; st < steps; ++st) {
-                at[st] = pos;
-                for (int q = 0; q < T; ++q) {
-                    size_t &hq = hist[(size_t)q * steps + st];
-                    const size_t c = hq;
-                    hq = pos;
-                    pos += c;
-                }
-                next_ext[st] = pos;
-                pos += ext_cnt[st];
-            }
-            at[steps] = pos;
-            for (const auto &x : ext) out_id[next_ext[(size_t)(x.first - t0)]++] = x.second;
-        }
-        if (bar) bar->wait();
-        for (size_t i = chunk_begin(k); i < chunk_begin(k + 1); ++i) out_id[h[(size_t)(ts[i] - t0)]++] = ids[i];
-        if (bar) bar->wait();
-        // steps whose first entry falls in this thread's share of the output
-        const size_t lo = total * (size_t)k / (size_t)T, hi = total * (size_t)(k + 1) / (size_t)T;
-        size_t st = (size_t)(std::lower_bound(at.begin(), at.end() - 1, lo) - at.begin());
-        for (; st < steps && at[st] < hi; ++st) {
-            std::sort(out_id + at[st], out_id + at[st + 1]);
-            std::fill(out_t + at[st], out_t + at[st + 1], t0 + (int)st);
-        }
+// Order this call's n device raster entries by (step, id) into ord_ids /
+// ord_t; returns the number of ordered entries in *n_out.
+nbg_status order_raster(nbg_engine *e, unsigned n, int t0, int count, unsigned *n_out) {
+    *n_out = 0;
+    if (n == 0) return NBG_OK;
+    const int wp = (((e->N + 31) >> 5) + 3) & ~3;
+    const int chunk =
+        (int)std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)(e->raster_bitmap_words / (size_t)wp)));
+    auto tiles_of = [&](int steps) {
+        return (unsigned)(((size_t)steps * (size_t)wp + kRasterTileWords - 1) / kRasterTileWords);
     };
-    if (T == 1) {
-        body(0, nullptr);
+    const unsigned max_tiles = tiles_of(chunk);
+    if (e->rbm.n < (size_t)max_tiles * kRasterTileWords) NBG_CUDA(e->rbm.alloc((size_t)max_tiles * kRasterTileWords));
+    if (e->rtile.n < max_tiles) NBG_CUDA(e->rtile.alloc(max_tiles));
+    if (e->rbase.n < 1) NBG_CUDA(e->rbase.alloc(1));
+    if (e->ord_ids.n < n) {
+        NBG_CUDA(e->ord_ids.alloc(n));
+        NBG_CUDA(e->ord_t.alloc(n));
+    }
+    NBG_CUDA(cudaEventRecord(e->evr0, e->stream));
+    NBG_CUDA(cudaMemsetAsync(e->rbase.p, 0, sizeof(unsigned), e->stream));
+    const unsigned mark_grid =
+        (unsigned)std::min<size_t>(((size_t)n + kRasterThreads - 1) / kRasterThreads, (size_t)e->sm_count * 8);
+    int64_t launches = 0;
+    for (int c0 = 0; c0 < count; c0 += chunk) {
+        const int steps = std::min(chunk, count - c0);
+        const unsigned tiles = tiles_of(steps);
+        NBG_CUDA(cudaMemsetAsync(e->rbm.p, 0, (size_t)tiles * kRasterTileWords * sizeof(unsigned), e->stream));
+        k_raster_mark<<<mark_grid, kRasterThreads, 0, e->stream>>>(e->out_t.p, e->out_ids.p, n, t0 + c0, steps, wp,
+                                                                   (int)e->N, e->rbm.p);
+        k_raster_count<<<tiles, kRasterThreads, 0, e->stream>>>(reinterpret_cast<const uint4 *>(e->rbm.p),
+                                                                e->rtile.p);
+        k_raster_scan<<<1, kRasterScanThreads, 0, e->stream>>>(e->rtile.p, tiles, e->rbase.p);
+        k_raster_emit<<<tiles, kRasterThreads, 0, e->stream>>>(reinterpret_cast<const uint4 *>(e->rbm.p),
+                                                               e->rtile.p, wp, t0 + c0, e->ord_ids.p, e->ord_t.p);
+        launches += 4;
+    }
+    NBG_CUDA(cudaGetLastError());
+    NBG_CUDA(cudaEventRecord(e->evr1, e->stream));
+    NBG_CUDA(cudaMemcpyAsync(n_out, e->rbase.p, sizeof(unsigned), cudaMemcpyDeviceToHost, e->stream));
+    NBG_CUDA(cudaStreamSynchronize(e->stream));
+    float ms = 0.0f;
+    NBG_CUDA(cudaEventElapsedTime(&ms, e->evr0, e->evr1));
+    e->last_order_ms = ms;
+    e->last_order_launches = launches;
+    if (*n_out != n) return fail(NBG_ERR_STATE, "raster holds %u entries but %u distinct (step, neuron) pairs", n, *n_out);
+    return NBG_OK;
+}
+
+// Append one run call's raster, already in (step, id) order, to spk_t /
+// spk_id, merged with ext: the external spikes of recorded neurons, sorted
+// by (step, id) and never among the device entries.  Large appends copy on
+// up to 16 host threads.
+void append_raster(nbg_engine *e, const int *ts, const int *ids, size_t n,
+                   const std::vector<std::pair<int, int>> &ext) {
+    const size_t base = e->spk_id.size();
+    e->spk_id.resize(base + n + ext.size());
+    e->spk_t.resize(base + n + ext.size());
+    int *out_id = e->spk_id.data() + base, *out_t = e->spk_t.data() + base;
+    if (!ext.empty()) {
+        size_t i = 0, j = 0, o = 0;
+        while (i < n || j < ext.size()) {
+            const bool take_dev = j == ext.size() ||
+                                  (i < n && (ts[i] < ext[j].first || (ts[i] == ext[j].first && ids[i] < ext[j].second)));
+            if (take_dev) {
+                out_t[o] = ts[i];
+                out_id[o++] = ids[i++];
+            } else {
+                out_t[o] = ext[j].first;
+                out_id[o++] = ext[j++].second;
+            }
+        }
         return;
     }
-    Barrier bar(T);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = n >= ((size_t)1 << 20) ? (int)std::min(16u, hw) : 1;
+    auto body = [&](int k) {
+        const size_t lo = n * (size_t)k / (size_t)T, hi = n * (size_t)(k + 1) / (size_t)T;
+        std::memcpy(out_t + lo, ts + lo, (hi - lo) * sizeof(int));
+        std::memcpy(out_id + lo, ids + lo, (hi - lo) * sizeof(int));
+    };
     std::vector<std::thread> pool;
-    for (int k = 1; k < T; ++k) pool.emplace_back(body, k, &bar);
-    body(0, &bar);
+    for (int k = 1; k < T; ++k) pool.emplace_back(body, k);
+    body(0);
     for (auto &th : pool) th.join();
 }
 
@@ -1744,6 +1912,13 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
     chk(cudaEventCreate(&e->ev0), "event");
     chk(cudaEventCreate(&e->ev1), "event");
+    chk(cudaEventCreate(&e->evr0), "event");
+    chk(cudaEventCreate(&e->evr1), "event");
+    chk(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, e->device), "SM count");
+    if (const char *rb = std::getenv("NBG_RASTER_BITMAP_WORDS")) {
+        const long long v = std::atoll(rb);
+        if (v > 0) e->raster_bitmap_words = (size_t)v;
+    }
 
     chk(e->pop.upload(pop), "pop");
     chk(e->meta.upload(meta), "meta");
@@ -1818,6 +1993,8 @@ nbg_status nbg_destroy(nbg_engine *e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->graph) cudaGraphExecDestroy(e->graph);
     if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->evr0) cudaEventDestroy(e->evr0);
+    if (e->evr1) cudaEventDestroy(e->evr1);
     if (e->ev1) cudaEventDestroy(e->ev1);
     for (auto ev : e->tev)
         if (ev) cudaEventDestroy(ev);
@@ -2038,12 +2215,17 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     if (errv & kErrEventLog) return fail(NBG_ERR_OVERFLOW, "delivered-event log capacity exceeded");
     if (errv & kErrOverflow)
         return fail(NBG_ERR_OVERFLOW, "spike raster capacity (%lld) exceeded in this run call", (long long)cap);
-    // raster: the device's unordered (step, id) entries plus the external
-    // spikes of output neurons, bucketed by step and sorted by id within it
-    unsigned int ndev = 0;
+    // raster: the device's unordered (step, id) entries, ordered on the
+    // device, downloaded through pinned staging buffers and merged with the
+    // external spikes of output neurons
+    unsigned ndev = 0;
     NBG_CUDA(cudaMemcpy(&ndev, e->cursor.p, sizeof(ndev), cudaMemcpyDeviceToHost));
-    // downloaded into pinned staging buffers (grown by half again when short)
-    if ((size_t)ndev > e->pin_cap) {
+    {
+        nbg_status os = order_raster(e, ndev, t0, count, &ndev);
+        if (os != NBG_OK) return os;
+    }
+    const auto h0 = std::chrono::steady_clock::now();
+    if ((size_t)ndev > e->pin_cap) { // grown by half again when short
         if (e->pin_ids) cudaFreeHost(e->pin_ids);
         if (e->pin_t) cudaFreeHost(e->pin_t);
         e->pin_ids = e->pin_t = nullptr;
@@ -2054,15 +2236,19 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         e->pin_cap = cap;
     }
     if (ndev > 0) {
-        NBG_CUDA(cudaMemcpy(e->pin_ids, e->out_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
-        NBG_CUDA(cudaMemcpy(e->pin_t, e->out_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(e->pin_ids, e->ord_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(e->pin_t, e->ord_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
     }
+    const auto h1 = std::chrono::steady_clock::now();
     {
-        std::vector<std::pair<int, int>> ext_rec; // external spikes of recorded neurons
+        std::vector<std::pair<int, int>> ext_rec; // external spikes of recorded neurons, (step, id) order
         for (const auto &x : ext_due)
             if (e->layers[e->pop_host[x.second]].record) ext_rec.push_back(x);
-        assemble_raster(e, e->pin_t, e->pin_ids, (size_t)ndev, ext_rec, t0, count);
+        append_raster(e, e->pin_t, e->pin_ids, (size_t)ndev, ext_rec);
     }
+    const auto h2 = std::chrono::steady_clock::now();
+    e->last_download_ms = std::chrono::duration<double, std::milli>(h1 - h0).count();
+    e->last_append_ms = std::chrono::duration<double, std::milli>(h2 - h1).count();
     if (ntr > 0) {
         const size_t rb = e->trace_rows.size();
         e->trace_rows.resize(rb + (size_t)count * ntr);
@@ -2407,6 +2593,16 @@ nbg_status nbg_profile(nbg_engine *e, double *total_ms, double *update_ms, doubl
     if (update_ms) *update_ms = e->last_upd_ms;
     if (propagate_ms) *propagate_ms = e->last_prop_ms;
     if (launches) *launches = e->last_launches;
+    return NBG_OK;
+}
+
+nbg_status nbg_raster_profile(nbg_engine *e, double *order_ms, double *download_ms, double *append_ms,
+                              int64_t *order_launches) {
+    if (!e) return fail(NBG_ERR_INVALID, "null engine");
+    if (order_ms) *order_ms = e->last_order_ms;
+    if (download_ms) *download_ms = e->last_download_ms;
+    if (append_ms) *append_ms = e->last_append_ms;
+    if (order_launches) *order_launches = e->last_order_launches;
     return NBG_OK;
 }
 

@@ -626,8 +626,13 @@ class Simulation:
                                         ctypes.byref(n)))
         acc = getattr(self, "_prof_total", None) or {"total_device_ms": 0.0, "total_kernel_launches": 0,
                                                      "run_calls": 0, "simulated_steps": 0}
+        ro, rd, ra = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        rn = ctypes.c_int64()
+        _lib.check(self.lib.nbg_raster_profile(self._h, ctypes.byref(ro), ctypes.byref(rd), ctypes.byref(ra),
+                                               ctypes.byref(rn)))
         return {"device_ms": tot.value, "update_kernel_ms": upd.value, "propagate_kernel_ms": prop.value,
-                "kernel_launches": n.value, **acc}
+                "kernel_launches": n.value, "raster_order_ms": ro.value, "raster_order_launches": rn.value,
+                "raster_download_ms": rd.value, "raster_append_ms": ra.value, **acc}
 
     def reset_bench_profiling(self) -> "Simulation":
         """Zero the totals of bench_profiling_snapshot."""
