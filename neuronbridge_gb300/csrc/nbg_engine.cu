@@ -190,6 +190,7 @@ __device__ __forceinline__ float izh_g(float a, float b, float v, float u) { ret
 
 struct NeuronRegs {
     float v, u, gexc, ginh, iext;
+    float lif_cur; // legacy LIF: 0 + R * I_ext / tau, constant over a launch (I_ext changes between launches)
     int last;
 };
 
@@ -440,9 +441,7 @@ __device__ __forceinline__ bool update_neuron(const NetDev &n, const Model &M, N
             r.v = nv;
             return false;
         }
-        float cur = 0.0f;
-        cur = cur + M.p[3] * r.iext / M.p[1];
-        float aux = (r.last > M.ip) ? cur + (M.p[0] - r.v) / M.p[1] : 0.0f;
+        float aux = (r.last > M.ip) ? r.lif_cur + (M.p[0] - r.v) / M.p[1] : 0.0f;
         r.v = r.v + aux * n.dt;
         r.last += 1;
         if (r.v > M.p[2]) {
@@ -758,6 +757,9 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
         r.ginh = n.ginh[j];
         r.iext = n.iext[j];
         r.last = n.last[j];
+        r.lif_cur = 0.0f;
+        if (S::has(NBG_MODEL_LIF_VJ) && L.model == NBG_MODEL_LIF_VJ) // current_dV += R * I / tau (two roundings)
+            r.lif_cur = r.lif_cur + L.p[3] * r.iext / L.p[1];
     }
     // noisy RK4 neurons: per-neuron noise key (the per-step draw is made in the step loop)
     const bool noisy = S::has(NBG_MODEL_IZH_RK4) && active && L.model == NBG_MODEL_IZH_RK4 && L.p[5] != 0.0f;
