@@ -66,6 +66,10 @@ BATCHED_TRAFFIC_BYTES = 2.206e9  # 238.3 MB on 282,235 LIF neurons x 2,612,540 /
 # DRAM bytes (read + write) of one dense step launch (64 x 8192, delivery and
 # update) from an ncu capture with a cold L2
 DENSE_TRAFFIC_BYTES = 277.5e6
+# device -> host bytes of a run call besides its raster entries (8 B each: step
+# and id) and traces: error word, raster cursor, ordered-entry count (4 B each)
+# and the delivered-event counter read by num_events (8 B)
+RUN_CALL_D2H_BYTES = 4 + 4 + 4 + 8
 
 
 def _peaks():
@@ -257,7 +261,8 @@ def bench_lif(args) -> dict:
                              "unit": "GB/s", "frac": upd_bytes / upd / 1e9 / peak, "peak_kind": kind,
                              "traffic": None},
                    e2e={"value": ev / wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
-                        "d2h_bytes_per_step": int(8 * spikes / args.steps + 4 * len(trace_ids) * cfg.steps)},
+                        "d2h_bytes_per_step": int(8 * spikes / args.steps + 4 * len(trace_ids) * cfg.steps
+                                                 + RUN_CALL_D2H_BYTES)},
                    gpu_launches=int(launches), clocks=clk)
 
 
@@ -295,6 +300,7 @@ def bench_batched(args) -> dict | None:
     ev = dev = wall = 0.0
     launches = 0
     raster = {"order_ms": 0.0, "download_ms": 0.0, "append_ms": 0.0, "order_launches": 0}
+    raster_entries = 0
     tune = {"choice": None}
     block_steps = None
     clk = None
@@ -321,6 +327,7 @@ def bench_batched(args) -> dict | None:
             launches += p["kernel_launches"]
             for k in raster:
                 raster[k] += p["raster_" + k]
+            raster_entries += sim._num_raster()  # downloaded as (step, id) int32 pairs
             sim.clear_spikes()
         clk = clocks.stop()
         block_steps = sim.block_steps
@@ -375,7 +382,7 @@ def bench_batched(args) -> dict | None:
                           "wall_s_per_1000_steps": p_wall_all},
                    speedup_vs_plain=value / plain,
                    e2e={"value": ev_all / wall_all, "unit": "synaptic events/s", "h2d_bytes_per_step": 16,
-                        "d2h_bytes_per_step": None},
+                        "d2h_bytes_per_step": int(8 * raster_entries / max(1, args.steps) + RUN_CALL_D2H_BYTES)},
                    raster_per_run_call={k: v / max(1, args.steps) for k, v in raster.items()},
                    gpu_launches=int(launches + raster["order_launches"]), clocks=clk)
     line["n_gpus"] = world
@@ -593,7 +600,7 @@ def main() -> None:
     peak, peak_kind = _peaks()
     achieved = upd_bytes / tot_upd / 1e9 if tot_upd > 0 else None
     value = tot_ev_all / tot_dev
-    d2h = 4 * (tot_spk / args.steps) + 4 * (args.sim_steps) + 8 + 8 + 4
+    d2h = 8 * (tot_spk / args.steps) + RUN_CALL_D2H_BYTES
     line = {
         "metric": "synaptic events/s", "value": value, "unit": "synaptic events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_dev / args.steps,
