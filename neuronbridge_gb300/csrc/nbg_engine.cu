@@ -1440,6 +1440,8 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster_emit(const uint4 *__r
 // ord_t; returns the number of ordered entries in *n_out.
 nbg_status order_raster(nbg_engine *e, unsigned n, int t0, int count, unsigned *n_out) {
     *n_out = 0;
+    e->last_order_ms = 0.0;
+    e->last_order_launches = 0;
     if (n == 0) return NBG_OK;
     const int wp = (((e->N + 31) >> 5) + 3) & ~3;
     const int chunk =

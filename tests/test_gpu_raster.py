@@ -57,3 +57,13 @@ def test_raster_order_large_batch(oracle_lib):
     rt, ri = _oracle_raster(union, cfg, 200)
     assert len(t) > (1 << 16)
     assert np.array_equal(t, rt) and np.array_equal(i, ri)
+
+
+def test_raster_profile_of_a_silent_call():
+    """A run call that records no spike orders nothing and says so."""
+    net, cfg = workloads.plain_lif(n=200, steps=50, rate_hz=0.0)
+    sim = nb.Simulation(net, cfg)
+    sim.run(50)
+    snap = sim.bench_profiling_snapshot()
+    assert len(sim.spike_raster()[0]) == 0
+    assert snap["raster_order_launches"] == 0 and snap["raster_order_ms"] == 0.0
