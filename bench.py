@@ -129,9 +129,45 @@ def _dist():
     return world, rank, local
 
 
+def _host_cpu() -> str:
+    """Host CPU model (lscpu / /proc/cpuinfo) for the CPU-side numbers."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for key in ("Model name:", "BIOS Model name:"):
+            for line in out.splitlines():
+                if line.strip().startswith(key):
+                    return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def _post_fanout(desc) -> np.ndarray:
     """plastic in-degree per neuron"""
     return np.bincount(desc.target[desc.rule >= 0], minlength=desc.neuron_count)
+
+
+def headline_config(sim_steps: int, world: int) -> dict:
+    """`config` of the headline workload, shared by both arms (the GPU engine
+    and the CPU reference arm) so that they describe the same work.  The
+    launch shape the GPU arm tunes is reported beside it, not in it."""
+    from neuronbridge_gb300 import workloads
+
+    return {"workload": "izhikevich_stdp_100k", "neurons": 100_000, "synapses": 10_000_000,
+            "plastic_synapses": 7_999_283, "sim_steps_per_step": sim_steps, "dt_ms": 0.1, "integrator": "rk4",
+            "noise_sigma_per_step": round(workloads.IZH_NOISE_PER_MS * float(np.sqrt(1.0 / 0.1)), 4),
+            "noise": "N(0, 5^2) per ms as a per-step Irwin-Hall(12) draw, sigma 5*sqrt(1 ms/dt) = 15.81 per "
+                     "0.1-ms step (sigma 5 per step leaves the network silent; see sigma5_per_step)",
+            "connectivity_rng": "numpy PCG64 seed 1 (not mt19937_64); in-degree 100, sources drawn with "
+                                "replacement (about 5% multapses), self excluded",
+            "l2": "flushed between timed iterations (256 MiB write)",
+            "parallelism": "replicas" if world > 1 else "single"}
 
 
 def cpu_baseline_sample(sim_steps: int = 3000) -> dict:
@@ -153,6 +189,99 @@ def cpu_baseline_sample(sim_steps: int = 3000) -> dict:
             "neuron_steps_per_s": 100_000 * (sim_steps + 1) / dt, "seconds": dt}
 
 
+def sigma5_sample(args, local: int, choice: dict | None) -> dict:
+    """The headline network with the literal per-step noise sigma of 5 (the
+    same connectivity, seeds and launch shape): the network stays silent, so
+    a step is the neuron update and the empty drain alone.  Three run calls of
+    args.sim_steps after one warm-up call, CUDA events on the engine stream."""
+    import neuronbridge_gb300 as nb
+    from neuronbridge_gb300 import workloads
+
+    net, cfg = workloads.izhikevich_stdp(noise_sigma=5.0)
+    sim = nb.Simulation(net, cfg, device=local, seed=2)
+    if choice:
+        sim.set_launch(int(choice["threads_per_block"]), int(choice["block_steps"]))
+    sim.run(args.sim_steps)
+    sim.clear_spikes()
+    dev = 0.0
+    launches = ev = spikes = 0
+    calls = 3
+    for _ in range(calls):
+        e0 = sim.num_events
+        sim.run(args.sim_steps)
+        p = sim.bench_profiling_snapshot()
+        dev += p["device_ms"] / 1e3
+        launches += p["kernel_launches"]
+        ev += sim.num_events - e0
+        spikes += len(sim.spike_raster()[0])
+        sim.clear_spikes()
+    sim.close()
+    n = 100_000
+    return {"noise_sigma_per_step": 5.0, "neuron_steps_per_s": n * args.sim_steps * calls / dev,
+            "synaptic_events_per_s": ev / dev, "spikes": int(spikes), "sim_steps": args.sim_steps * calls,
+            "avg_launch_us": 1e6 * dev / max(1, launches), "launches": int(launches)}
+
+
+def phase_split(neuron_bytes: float, delivery_bytes: float, dev_s: float, launches: int, silent: dict,
+                peak: float) -> dict:
+    """Roofline fractions of the two phases of k_update.  The neuron update
+    (with the drain of an empty arrival ring) is timed on the silent sigma-5
+    network, the same launches with no spike and no arrival; delivery + STDP
+    is the rest of the headline launch.  Each phase's algorithmic bytes over
+    its time, against the measured HBM peak."""
+    t_launch = dev_s / max(1, launches)
+    t_upd = silent["avg_launch_us"] * 1e-6
+    t_del = t_launch - t_upd
+    upd = neuron_bytes / max(1, launches) / t_upd / 1e9
+    out = {"method": "update = launch time of the same network at noise sigma 5 per step (silent); "
+                     "delivery + STDP = headline launch time minus that",
+           "update": {"launch_us": 1e6 * t_upd, "achieved": upd, "frac": upd / peak,
+                      "bytes_per_launch": neuron_bytes / max(1, launches)}}
+    if t_del > 0:
+        dl = delivery_bytes / max(1, launches) / t_del / 1e9
+        out["delivery_stdp"] = {"launch_us": 1e6 * t_del, "achieved": dl, "frac": dl / peak,
+                                "bytes_per_launch": delivery_bytes / max(1, launches)}
+    return out
+
+
+def fp64_error_sample(local: int, steps: int = 1000) -> dict:
+    """FP32 error against the FP64 oracle on the headline network: the
+    engine's first `steps` steps (a fresh simulation, membrane potential of
+    ten neurons every step) against the oracle's FP64 build of the same
+    discretised dynamics.  The oracle is the checker here, not the measured
+    path.  The network is chaotic, so the rasters part at some step; the
+    membrane error is taken over the steps before it."""
+    import oracle
+    import neuronbridge_gb300 as nb
+    from neuronbridge_gb300 import workloads
+
+    net, cfg = workloads.izhikevich_stdp()
+    trace_ids = np.arange(0, 100_000, 10_000)
+    sim = nb.Simulation(net, cfg, device=local, seed=2)
+    sim.set_trace(trace_ids)
+    sim.run(steps)
+    t32, i32 = sim.spike_raster()
+    tr32 = sim.traces().astype(np.float64)
+    sim.close()
+    o = oracle.OracleNet(net.to_native().flat(cfg.timestep, seed=2), precision=64).set_threads(os.cpu_count() or 1)
+    o.set_trace(trace_ids)
+    o.run(steps)
+    t64, i64 = o.spikes()
+    tr64 = o.traces()
+    k32 = np.unique(t32.astype(np.int64) << 32 | i32.astype(np.int64))
+    k64 = np.unique(t64.astype(np.int64) << 32 | i64.astype(np.int64))
+    diff = np.setxor1d(k32, k64, assume_unique=True)
+    fd = None if len(diff) == 0 else int(diff.min() >> 32)
+    upto = tr32.shape[0] if fd is None else fd
+    err = np.abs(tr32[:upto] - tr64[:upto])
+    rel = err / np.maximum(np.abs(tr64[:upto]), 1e-30)
+    return {"updates": int(tr32.shape[0]), "traced_neurons": len(trace_ids),
+            "first_raster_divergence_step": fd, "steps_compared": int(upto),
+            "membrane_max_abs_mV": float(err.max()), "membrane_median_abs_mV": float(np.median(err)),
+            "membrane_max_rel": float(rel.max()), "spikes_fp32": int(len(k32)), "spikes_fp64": int(len(k64)),
+            "spike_pairs_differing": int(len(diff))}
+
+
 def run_reference(args) -> None:
     world, rank, _ = _dist()
     if rank != 0:
@@ -165,7 +294,11 @@ def run_reference(args) -> None:
     cores = os.cpu_count() or 1
     net, cfg = workloads.izhikevich_stdp()
     o = oracle.OracleNet(net.to_native().flat(cfg.timestep, seed=2)).set_threads(cores)
-    sample = 1000  # simulation steps per benchmark step: a bounded sample
+    # the same windows as the GPU arm: W warm-up run calls then K timed ones,
+    # each args.sim_steps simulation steps, from the same initial state; a
+    # 256 MiB host write between timed windows, as the GPU arm flushes its L2
+    sample = args.sim_steps
+    flush = np.empty(256 * 1024 * 1024 // 8, np.float64)
     for k in range(args.warmup + args.steps):
         e0 = o.num_events
         t0 = time.perf_counter()
@@ -174,18 +307,20 @@ def run_reference(args) -> None:
         if k >= args.warmup:
             per_step.append(dt)
             events += o.num_events - e0
+            flush.fill(1.0)
     total = sum(per_step)
     value = events / total
     line = {
         "impl": "reference", "metric": "synaptic events/s", "value": value, "unit": "synaptic events/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "izhikevich_stdp_100k", "neurons": 100_000, "synapses": 10_000_000,
-                   "sim_steps_per_step": sample, "dt_ms": 0.1},
+        "config": headline_config(sample, world),
         "cpu_baseline": {"value": value, "unit": "synaptic events/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample} simulation steps per benchmark step of the 100k/10M network, "
-                                   "oracle FP32 restatement (the reference's CPU path does not build here: "
-                                   f"it needs Boost and its CMake build), OpenMP over {cores} host threads"},
+                         "host_cpu": _host_cpu(),
+                         "sample": f"the GPU arm's windows: {args.warmup} warm-up and {args.steps} timed run calls "
+                                   f"of {sample} simulation steps of the 100k/10M network, oracle FP32 restatement "
+                                   "(the reference's CPU path does not build here: it needs Boost and its CMake "
+                                   f"build), OpenMP over {cores} host threads"},
         "e2e": {"value": value, "unit": "synaptic events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -345,19 +480,21 @@ def bench_batched(args) -> dict | None:
         p_ev += s.num_events - e0
         p_dev += s.bench_profiling_snapshot()["device_ms"] / 1e3
         s.close()
+    # the Poisson layers have no inputs: the engine evaluates them inline at
+    # their targets, so the neuron-steps are the LIF neurons'
+    upd_bytes = BYTES_PER_LIF_NEURON_STEP * n_lif * cfg.steps * args.steps + BYTES_PER_STATIC_EVENT * ev
     dev_dev = f"cuda:{local}" if world > 1 else None
-    (dev_all, wall_all, p_dev_all, p_wall_all), (ev_all, p_ev_all) = aggregate(
-        [dev, wall, p_dev, p_wall], [ev, p_ev], device=dev_dev)
+    (dev_all, wall_all, p_dev_all, p_wall_all), (ev_all, p_ev_all, bytes_all) = aggregate(
+        [dev, wall, p_dev, p_wall], [ev, p_ev, upd_bytes], device=dev_dev)
     if rank != 0:
         return None
     value = ev_all / dev_all
     plain = p_ev_all / p_dev_all
-    # the Poisson layers have no inputs: the engine evaluates them inline at
-    # their targets, so the neuron-steps are the LIF neurons' (rank 0's share
-    # for the kernel roofline)
-    upd_bytes = BYTES_PER_LIF_NEURON_STEP * n_lif * cfg.steps * args.steps + BYTES_PER_STATIC_EVENT * ev
     peak, kind = _peaks()
     per_launch = launches / args.steps
+    # per GPU: every rank's algorithmic bytes over the slowest rank's device
+    # time, divided by the ranks (the same totals and clock as `value`)
+    achieved = bytes_all / dev_all / world / 1e9
     loads = shard_loads(sizes, shards)
     config = {"workload": f"batched_lif_{args.instances}", "instances": args.instances,
               "lif_neurons": int(sizes.sum()), "sim_steps_per_step": cfg.steps, "block_steps": block_steps,
@@ -372,8 +509,10 @@ def bench_batched(args) -> dict | None:
                    neuron_steps_per_s=int(sizes.sum()) * cfg.steps * args.steps / dev_all,
                    roofline={"bound": "hbm", "kernel": "k_update<Spec<1, 0>> (LIF, static; Poisson generators "
                                                        "packed eight per thread)",
-                             "achieved": upd_bytes / dev / 1e9, "peak": peak, "unit": "GB/s",
-                             "frac": upd_bytes / dev / 1e9 / peak, "peak_kind": kind,
+                             "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": kind,
+                             "scope": "per GPU" if world == 1 else
+                             f"per GPU: all {world} ranks' bytes / slowest rank's time / {world}",
                              "traffic": (BATCHED_TRAFFIC_BYTES if args.instances == 256 and world == 1 else None),
                              "traffic_unit": "bytes per launch (ncu on 32 instances, scaled by units)",
                              "algorithmic_bytes_per_launch": upd_bytes / (per_launch * args.steps),
@@ -594,11 +733,13 @@ def main() -> None:
     n = desc.neuron_count
     sim_steps = args.steps * args.sim_steps
     plastic_frac = float(np.mean(desc.rule >= 0))
-    upd_bytes = (BYTES_PER_NEURON_STEP * n * sim_steps
-                 + tot_ev * (plastic_frac * BYTES_PER_PLASTIC_EVENT + (1 - plastic_frac) * BYTES_PER_STATIC_EVENT)
-                 + BYTES_PER_POST_UPDATE * tot_post)
+    neuron_bytes = BYTES_PER_NEURON_STEP * n * sim_steps
+    delivery_bytes = (tot_ev * (plastic_frac * BYTES_PER_PLASTIC_EVENT + (1 - plastic_frac) * BYTES_PER_STATIC_EVENT)
+                      + BYTES_PER_POST_UPDATE * tot_post)
+    upd_bytes = neuron_bytes + delivery_bytes
     peak, peak_kind = _peaks()
     achieved = upd_bytes / tot_upd / 1e9 if tot_upd > 0 else None
+    silent = sigma5_sample(args, local, tune["choice"])
     value = tot_ev_all / tot_dev
     d2h = 8 * (tot_spk / args.steps) + RUN_CALL_D2H_BYTES
     line = {
@@ -606,12 +747,8 @@ def main() -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded network, in-kernel noise)",
-        "config": {"workload": "izhikevich_stdp_100k", "neurons": n, "synapses": int(len(desc.source)),
-                   "plastic_synapses": int(np.sum(desc.rule >= 0)), "sim_steps_per_step": args.sim_steps,
-                   "dt_ms": 0.1, "integrator": "rk4", "block_steps": sim.block_steps,
-                   "tuned": tune["choice"],
-                   "l2": "flushed between timed iterations (256 MiB write)", "parallelism": "replicas" if world > 1
-                   else "single"},
+        "config": headline_config(args.sim_steps, world),
+        "launch_shape": {"block_steps": sim.block_steps, "tuned": tune["choice"]},
         "neuron_steps_per_s": n * sim_steps * world / tot_dev,
         "spikes_per_s_simulated": tot_spk / (sim_steps * 1e-4) / n,
         "roofline": {"bound": "hbm", "kernel": "k_update (drain + RK4 + STDP + spike propagation)",
@@ -621,6 +758,8 @@ def main() -> None:
                      "traffic_unit": "bytes per launch (ncu, cold L2)",
                      "algorithmic_bytes_per_launch": upd_bytes / max(1, launches),
                      "avg_update_launch_us": 1e6 * tot_upd / max(1, launches)},
+        "phases": phase_split(neuron_bytes, delivery_bytes, tot_upd, launches, silent, peak),
+        "sigma5_per_step": silent,
         "e2e": {"value": tot_ev_all / tot_wall, "unit": "synaptic events/s", "h2d_bytes_per_step": 4 + 8 + 4,
                 "d2h_bytes_per_step": int(d2h)},
         "raster_per_run_call": {k: v / args.steps for k, v in raster.items()},
@@ -629,6 +768,7 @@ def main() -> None:
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
+        line["fp64_error"] = fp64_error_sample(local)
     print(json.dumps(line), flush=True)
 
 

@@ -291,7 +291,9 @@ nbg_status nbg_profile(nbg_engine *e, double *total_ms, double *update_ms, doubl
  * download to the host and the append to the recorded raster (host wall
  * time).  The reference records output spikes from its host event loop
  * (communication/src/ArrayOutputSpikeDriver.cpp); here they are this
- * separate phase after the step loop. */
+ * separate phase after the step loop.  If the device ordering fails (its
+ * buffers cannot be allocated), nbg_run downloads the unordered entries and
+ * orders them on the host instead, and order_launches reads -1. */
 nbg_status nbg_raster_profile(nbg_engine *e, double *order_ms, double *download_ms, double *append_ms,
                               int64_t *order_launches);
 

@@ -77,9 +77,17 @@ nbg_status nbg_dense_profile(nbg_dense *d, double *total_ms, double *delivery_ms
  *   neurons         a multiple of 128, at most NBG_DENSE_NOALLOC_MAX_NEURONS
  *                   (larger sizes are rejected with NBG_ERR_INVALID)
  *
+ * w_hi_t, w_lo_t and spikes must be 16-byte aligned (the kernel reads them
+ * with 16-byte copies) and out 4-byte aligned; a misaligned pointer, such as
+ * an offset view into a larger tensor, is rejected with NBG_ERR_INVALID before
+ * anything is launched.
+ *
  * The first call on a device looks up the scratch array's device address
- * there (with that device current); make that first call before any stream
- * capture.  Every call shares the one scratch array, so calls that overlap on
+ * there (with that device current) and keeps it for the life of the process;
+ * make that first call before any stream capture.  The address is not valid
+ * across cudaDeviceReset (the module is loaded again and the array may move),
+ * so do not use this function after resetting a device it has already run
+ * on.  Every call shares the one scratch array, so calls that overlap on
  * the GPU (different streams, or different host threads on the same device)
  * race: order them on one stream.  The scratch needs no clearing -- each call
  * writes every partial sum it reads. */

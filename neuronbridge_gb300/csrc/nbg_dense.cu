@@ -709,6 +709,10 @@ __global__ void k_sum_split_partials(const float *__restrict__ part, float *__re
 extern "C" nbg_status nbg_dense_deliver_noalloc(const void *w_hi_t, const void *w_lo_t, const void *spikes,
                                                 float *out, int neurons, void *stream) {
     if (!w_hi_t || !w_lo_t || !spikes || !out) return nbg_fail(NBG_ERR_INVALID, "null argument");
+    // the GEMM reads all three inputs with 16-byte cp.async copies
+    if (((uintptr_t)w_hi_t | (uintptr_t)w_lo_t | (uintptr_t)spikes) & 15u)
+        return nbg_fail(NBG_ERR_INVALID, "w_hi_t, w_lo_t and spikes must be 16-byte aligned");
+    if ((uintptr_t)out & 3u) return nbg_fail(NBG_ERR_INVALID, "out must be 4-byte aligned");
     if (neurons <= 0 || neurons % kBM != 0 || (neurons / kSplitK) % kBK != 0)
         return nbg_fail(NBG_ERR_INVALID, "neurons must be a positive multiple of %d", kBM);
     if (neurons > NBG_DENSE_NOALLOC_MAX_NEURONS)

@@ -993,6 +993,10 @@ struct nbg_engine {
     size_t pin_cap = 0;
     int sm_count = 1;
     size_t raster_bitmap_words = kRasterBitmapWords;
+    // host-side fault injection (NBG_RASTER_ORDER_FAIL, read at creation):
+    // the device ordering reports an allocation failure, which exercises the
+    // host fallback of nbg_run
+    bool raster_order_fail = false;
     // raster ordering: per-step spike bitmap, tile sums / positions, running
     // base, ordered entries; timings of the last run call's raster phases
     DevBuf<unsigned int> rbm, rtile, rbase;
@@ -1450,6 +1454,8 @@ nbg_status order_raster(nbg_engine *e, unsigned n, int t0, int count, unsigned *
         return (unsigned)(((size_t)steps * (size_t)wp + kRasterTileWords - 1) / kRasterTileWords);
     };
     const unsigned max_tiles = tiles_of(chunk);
+    if (e->raster_order_fail)
+        return fail(NBG_ERR_CUDA, "raster bitmap: %s (injected)", cudaGetErrorString(cudaErrorMemoryAllocation));
     if (e->rbm.n < (size_t)max_tiles * kRasterTileWords) NBG_CUDA(e->rbm.alloc((size_t)max_tiles * kRasterTileWords));
     if (e->rtile.n < max_tiles) NBG_CUDA(e->rtile.alloc(max_tiles));
     if (e->rbase.n < 1) NBG_CUDA(e->rbase.alloc(1));
@@ -1923,6 +1929,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
         const long long v = std::atoll(rb);
         if (v > 0) e->raster_bitmap_words = (size_t)v;
     }
+    if (const char *rf = std::getenv("NBG_RASTER_ORDER_FAIL")) e->raster_order_fail = std::atoi(rf) != 0;
 
     chk(e->pop.upload(pop), "pop");
     chk(e->meta.upload(meta), "meta");
@@ -2224,9 +2231,21 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     // external spikes of output neurons
     unsigned ndev = 0;
     NBG_CUDA(cudaMemcpy(&ndev, e->cursor.p, sizeof(ndev), cudaMemcpyDeviceToHost));
+    // The step loop has run and the engine's time has moved on, so a failed
+    // device ordering must not drop the call's spikes: the unordered entries
+    // are then downloaded and ordered on the host instead.
+    const int *ord_ids = e->ord_ids.p, *ord_t = e->ord_t.p;
+    bool host_order = false;
     {
-        nbg_status os = order_raster(e, ndev, t0, count, &ndev);
-        if (os != NBG_OK) return os;
+        unsigned nord = 0;
+        if (order_raster(e, ndev, t0, count, &nord) != NBG_OK) {
+            cudaGetLastError(); // an allocation failure is not sticky: clear it
+            NBG_CUDA(cudaStreamSynchronize(e->stream));
+            ord_ids = e->out_ids.p;
+            ord_t = e->out_t.p;
+            host_order = true;
+            e->last_order_launches = -1;
+        }
     }
     const auto h0 = std::chrono::steady_clock::now();
     if ((size_t)ndev > e->pin_cap) { // grown by half again when short
@@ -2240,8 +2259,18 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
         e->pin_cap = cap;
     }
     if (ndev > 0) {
-        NBG_CUDA(cudaMemcpy(e->pin_ids, e->ord_ids.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
-        NBG_CUDA(cudaMemcpy(e->pin_t, e->ord_t.p, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(e->pin_ids, ord_ids, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+        NBG_CUDA(cudaMemcpy(e->pin_t, ord_t, ndev * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    if (host_order && ndev > 1) { // (step, id) order on the host
+        std::vector<uint64_t> key((size_t)ndev);
+        for (size_t k = 0; k < ndev; ++k)
+            key[k] = ((uint64_t)(uint32_t)e->pin_t[k] << 32) | (uint32_t)e->pin_ids[k];
+        std::sort(key.begin(), key.end());
+        for (size_t k = 0; k < ndev; ++k) {
+            e->pin_t[k] = (int)(key[k] >> 32);
+            e->pin_ids[k] = (int)(uint32_t)key[k];
+        }
     }
     const auto h1 = std::chrono::steady_clock::now();
     {

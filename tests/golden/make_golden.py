@@ -1,8 +1,9 @@
 """Generate golden known-answer vectors from the reference's own KAT script.
 
-Run in a checkout that has the reference at /root/reference (read-only):
+Run it in a checkout that has a copy of the reference project (read-only),
+giving the reference's root directory as the one argument:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py <reference-root>
 
 It never executes the reference script's module-level code (that code builds
 a Windows results directory and needs the compiled ``neuronbridge._core``).
@@ -133,4 +134,6 @@ def main(reference_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference-root>")
+    main(sys.argv[1])

@@ -9,6 +9,7 @@ run calls, invariance to launch shape, instance independence in a batch) are
 checked at larger sizes.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -101,16 +102,94 @@ def test_izhikevich_stdp_small_bit_exact(oracle_lib):
     assert not np.array_equal(gw["weight"], net.to_native().weight)  # STDP moved weights
 
 
-def test_izhikevich_full_size_short_horizon_bit_exact(oracle_lib):
-    net, cfg = workloads.izhikevich_stdp()  # 100k neurons, 10M synapses
+def test_izhikevich_full_size_1000_steps_bit_exact(oracle_lib):
+    """The headline network itself -- 100k neurons, 10M synapses (8M plastic),
+    delays 10..200 steps, noise, pair STDP -- over its first 1,000 steps
+    (1,001 updates): several recurrent round trips with STDP acting.  Raster,
+    the membrane potential of ten neurons at every step, the final v, u and
+    LastSpike of every neuron, and every synapse's weight, Apre, Apost and
+    last-update step are bit-identical to the oracle."""
+    net, cfg = workloads.izhikevich_stdp()
+    trace_ids = np.arange(0, 100_000, 10_000)
     sim = nb.Simulation(net, cfg, seed=2)
-    sim.run(400)
-    o = _oracle(net, cfg, seed=2)
-    o.run(400)
-    assert _raster_equal(sim.spike_raster(), _oracle_raster(o, net))
-    assert np.array_equal(sim.state_field(0), o.state(0).astype(np.float32))
-    gw = sim.weights()["weight"]
-    assert np.array_equal(gw, o.weights()[0].astype(np.float32))
+    sim.set_trace(trace_ids)
+    sim.run(1000)
+    o = _oracle(net, cfg, seed=2).set_threads(os.cpu_count() or 1)
+    o.set_trace(trace_ids)
+    o.run(1000)
+    assert sim.next_time == o.next_time == 1001
+    g_raster = sim.spike_raster()
+    assert len(g_raster[0]) > 50_000  # ~7 spikes per ms of the 100k network
+    assert _raster_equal(g_raster, _oracle_raster(o, net))
+    assert sim.num_events == o.num_events
+    tr = sim.traces()
+    assert tr.shape == (1001, 10)
+    assert np.array_equal(tr, o.traces().astype(np.float32))
+    for f in (0, 1, 6):  # v, u, LastSpike
+        assert np.array_equal(sim.state_field(f), o.state(f).astype(np.float32)), f
+    gw = sim.weights()
+    ow, oa, ob, ol = o.weights()
+    assert np.array_equal(gw["weight"], ow.astype(np.float32))
+    assert np.array_equal(gw["apre"], oa.astype(np.float32))
+    assert np.array_equal(gw["apost"], ob.astype(np.float32))
+    assert np.array_equal(gw["last_update"], ol)
+    plastic = net.to_native().rule >= 0
+    moved = gw["weight"][plastic] != np.float32(6.0)
+    assert moved.sum() > 100_000  # STDP acted on many synapses
+
+
+def _first_divergence(a, b):
+    """First step at which two (time, id) rasters hold different spike sets
+    (None if they are equal)."""
+    (ta, ia), (tb, ib) = a, b
+    ka = np.unique(ta.astype(np.int64) << 32 | ia.astype(np.int64))
+    kb = np.unique(tb.astype(np.int64) << 32 | ib.astype(np.int64))
+    diff = np.setxor1d(ka, kb, assume_unique=True)
+    return None if len(diff) == 0 else int(diff.min() >> 32)
+
+
+# FP32 against the FP64 oracle (the same discretised dynamics, every float
+# operation in double): the north star's membrane tolerance is 1e-5 relative.
+MEMBRANE_REL_TOL = 1e-5
+
+
+@pytest.mark.parametrize("config", ["plain_lif", "izhikevich_stdp"])
+def test_fp32_error_against_fp64_oracle(oracle_lib, config):
+    """The engine's FP32 run against the FP64 oracle.  The membrane traces of
+    ten neurons stay within MEMBRANE_REL_TOL of FP64 at every step up to the
+    first step at which the rasters differ.  Plain LIF: the rasters agree over
+    at least the first 1,000 steps (2,977 measured) and the final spike count
+    is within 0.01 %.  Izhikevich + STDP at 100k neurons is chaotic (noise,
+    recurrent excitation): one threshold crossing among 100k neurons flips
+    within the first 100 steps (step 48 measured), after which the spike
+    counts still agree within 0.1 % over 1,000 steps."""
+    import oracle
+
+    if config == "plain_lif":
+        net, cfg = workloads.plain_lif()
+        steps, trace_ids, kw = cfg.steps, np.arange(0, 1000, 100), {}
+    else:
+        net, cfg = workloads.izhikevich_stdp()
+        steps, trace_ids, kw = 1000, np.arange(0, 100_000, 10_000), {"seed": 2}
+    sim = nb.Simulation(net, cfg, **kw)
+    sim.set_trace(trace_ids)
+    sim.run(steps)
+    o64 = oracle.OracleNet(net.to_native().flat(cfg.timestep, **kw), precision=64).set_threads(os.cpu_count() or 1)
+    o64.set_trace(trace_ids)
+    o64.run(steps)
+    g, r = sim.spike_raster(), _oracle_raster(o64, net)
+    fd = _first_divergence(g, r)
+    upto = steps + 1 if fd is None else fd  # trace row k is step k
+    tr32, tr64 = sim.traces()[:upto].astype(np.float64), o64.traces()[:upto]
+    rel = np.abs(tr32 - tr64) / np.maximum(np.abs(tr64), 1e-30)
+    assert upto > 10 and rel.max() <= MEMBRANE_REL_TOL, (fd, rel.max())
+    n32, n64 = len(g[0]), len(r[0])
+    if config == "plain_lif":
+        assert fd is None or fd >= 1000, fd
+        assert abs(n32 - n64) <= 1e-4 * n64, (n32, n64)
+    else:
+        assert fd is None or fd >= 10, fd
+        assert abs(n32 - n64) <= 1e-3 * n64, (n32, n64)
 
 
 def test_conductance_izhikevich_kat_on_gpu():

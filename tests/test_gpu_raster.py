@@ -67,3 +67,20 @@ def test_raster_profile_of_a_silent_call():
     snap = sim.bench_profiling_snapshot()
     assert len(sim.spike_raster()[0]) == 0
     assert snap["raster_order_launches"] == 0 and snap["raster_order_ms"] == 0.0
+
+
+def test_raster_host_fallback_when_device_ordering_fails(oracle_lib, monkeypatch):
+    """The step loop has already advanced the engine when the raster is
+    ordered, so a failed device ordering (an allocation failure, injected on
+    the host with NBG_RASTER_ORDER_FAIL) falls back to ordering the
+    downloaded entries on the host: no spike of the call is lost."""
+    net, cfg = workloads.plain_lif(n=400, steps=300)
+    monkeypatch.setenv("NBG_RASTER_ORDER_FAIL", "1")
+    sim = nb.Simulation(net, cfg)
+    sim.run(120)
+    sim.run(180)
+    assert sim.bench_profiling_snapshot()["raster_order_launches"] == -1
+    t, i = sim.spike_raster()
+    rt, ri = _oracle_raster(net, cfg, 300)
+    assert len(t) > 0
+    assert np.array_equal(t, rt) and np.array_equal(i, ri)

@@ -61,3 +61,10 @@ def test_noalloc_delivery_matches_allocating_entry_point():
     big = 8192 + 128
     st = noalloc(w_hi_t.data_ptr(), w_lo_t.data_ptr(), s_dev.data_ptr(), out.data_ptr(), big, stream)
     assert st == 1 and b"no-allocation limit" in lib.nbg_last_error()
+
+    # an input that does not start on a 16-byte boundary (an offset view) is
+    # refused before any launch
+    st = noalloc(w_hi_t.data_ptr() + 2, w_lo_t.data_ptr(), s_dev.data_ptr(), out.data_ptr(), n, stream)
+    assert st == 1 and b"16-byte aligned" in lib.nbg_last_error()
+    st = noalloc(w_hi_t.data_ptr(), w_lo_t.data_ptr(), s_dev.data_ptr() + 8, out.data_ptr(), n, stream)
+    assert st == 1 and b"16-byte aligned" in lib.nbg_last_error()
