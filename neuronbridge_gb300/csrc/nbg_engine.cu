@@ -2234,11 +2234,14 @@ nbg_status nbg_run(nbg_engine *e, int steps) {
     // The step loop has run and the engine's time has moved on, so a failed
     // device ordering must not drop the call's spikes: the unordered entries
     // are then downloaded and ordered on the host instead.
-    const int *ord_ids = e->ord_ids.p, *ord_t = e->ord_t.p;
+    const int *ord_ids = nullptr, *ord_t = nullptr;
     bool host_order = false;
     {
         unsigned nord = 0;
-        if (order_raster(e, ndev, t0, count, &nord) != NBG_OK) {
+        if (order_raster(e, ndev, t0, count, &nord) == NBG_OK) { // ordering may have grown ord_ids / ord_t
+            ord_ids = e->ord_ids.p;
+            ord_t = e->ord_t.p;
+        } else {
             cudaGetLastError(); // an allocation failure is not sticky: clear it
             NBG_CUDA(cudaStreamSynchronize(e->stream));
             ord_ids = e->out_ids.p;

@@ -94,6 +94,7 @@ def _lib(prec: int):
                                   ctypes.c_float]),
             "dense_destroy": (None, [vp]),
             "dense_run": (ctypes.c_int, [vp, ctypes.c_int]),
+            "dense_set_threads": (None, [vp, ctypes.c_int]),
             "dense_num_steps": (ctypes.c_int64, [vp]),
             "dense_counts": (None, [vp, i32p]),
             "dense_state": (None, [vp, f64p, i32p, ctypes.POINTER(ctypes.c_uint8)]),
@@ -266,6 +267,11 @@ class OracleDense:
         if h:
             self._f("dense_destroy")(h)
             self.h = None
+
+    def set_threads(self, threads: int) -> "OracleDense":
+        """OpenMP threads over instances (results do not change)."""
+        self._f("dense_set_threads")(self.h, int(threads))
+        return self
 
     def run(self, steps: int) -> "OracleDense":
         if self._f("dense_run")(self.h, int(steps)) != 0:

@@ -975,7 +975,7 @@ void ORC(add_current)(void *hp, int t, int id, double value) {
  * (TimeDrivenLIF_Voltage_jump.cpp:49-86).  The first run performs N+1 updates.
  * ------------------------------------------------------------------------ */
 typedef struct {
-    int B, N, t_ref, next_t, ran;
+    int B, N, t_ref, next_t, ran, threads;
     REAL v_rest, tau, v_th, r, v_reset, i_ext, dt, drive_w;
     float drive_p;
     const float *w; /* borrowed: N x N */
@@ -1026,10 +1026,16 @@ void ORC(dense_destroy)(void *hp) {
     free(d);
 }
 
+/* Instances are independent (each its own V, LastSpike and spike row), so
+ * they run on OpenMP threads; every instance's arithmetic is the same
+ * sequential sum as on one thread. */
 static void dense_step(dense_t *d, int t) {
     const int N = d->N;
-    REAL *col = (REAL *)malloc((size_t)N * sizeof(REAL));
     int64_t nspk = 0;
+#pragma omp parallel num_threads(d->threads > 0 ? d->threads : 1) reduction(+ : nspk)
+    {
+    REAL *col = (REAL *)malloc((size_t)N * sizeof(REAL));
+#pragma omp for schedule(static)
     for (int b = 0; b < d->B; ++b) {
         const unsigned char *sb = d->s + (size_t)b * N;
         for (int j = 0; j < N; ++j) col[j] = K(0.0);
@@ -1062,11 +1068,12 @@ static void dense_step(dense_t *d, int t) {
             d->s_next[idx] = spk;
         }
     }
+    free(col);
+    }
     unsigned char *tmp = d->s;
     d->s = d->s_next;
     d->s_next = tmp;
     vpush(&d->counts, nspk);
-    free(col);
 }
 
 int ORC(dense_run)(void *hp, int steps) {
@@ -1079,6 +1086,7 @@ int ORC(dense_run)(void *hp, int steps) {
     return 0;
 }
 
+void ORC(dense_set_threads)(void *hp, int threads) { ((dense_t *)hp)->threads = threads; }
 int64_t ORC(dense_num_steps)(void *hp) { return ((dense_t *)hp)->counts.n; }
 void ORC(dense_counts)(void *hp, int *out) {
     dense_t *d = (dense_t *)hp;
