@@ -55,6 +55,57 @@ def build(force: bool = False) -> None:
         os.replace(out + ".tmp", out)
 
 
+_REF_DIR = os.path.join(_HERE, "_ref")
+_REF_STDP = os.path.join(_REF_DIR, "libnbg_ref_stdp.so")
+
+
+def build_ref() -> str | None:
+    """Compile the reference's own pair-STDP code path (its STDP.cpp,
+    STDP_State.cpp and the classes they use, from the reference tree, with
+    oracle/ref_stdp/Makefile) into oracle/_ref/.  The reference tree is the
+    Makefile's REF, or the NBG_REFERENCE_ROOT environment variable.  Returns
+    the library path, or None when the reference tree is not on this machine
+    (the recipe then has nothing to compile)."""
+    cmd = ["make", "-s", "-C", os.path.join(_HERE, "ref_stdp"), "-j4"]
+    root = os.environ.get("NBG_REFERENCE_ROOT")
+    if root:
+        cmd.append(f"REF={root}")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        if "No rule to make target" in r.stderr:
+            return None
+        raise RuntimeError("reference STDP build failed:\n" + r.stderr)
+    return _REF_STDP
+
+
+def ref_stdp_run(w0, wmax, max_ltp, ltp_tau, max_ltd, ltd_tau, dt, pre, post):
+    """Replay a pre/post event schedule through the reference's own STDP
+    (oracle/_ref, see build_ref).  ``pre`` is [ticks][connections] and
+    ``post`` [ticks] (0/1).  Returns (weights after every tick
+    [ticks][connections], Apre, Apost, LastUpdate) as float32 / int32."""
+    lib = ctypes.CDLL(_REF_STDP)
+    f32p, i32p, u8p = (ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int),
+                       ctypes.POINTER(ctypes.c_uint8))
+    fn = lib.nbgref_stdp_run
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, f32p, f32p, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                   ctypes.c_float, ctypes.c_int, u8p, u8p, f32p, f32p, f32p, i32p]
+    w0 = np.ascontiguousarray(w0, np.float32)
+    wmax = np.ascontiguousarray(wmax, np.float32)
+    pre = np.ascontiguousarray(pre, np.uint8)
+    post = np.ascontiguousarray(post, np.uint8)
+    ticks, n = pre.shape
+    traj = np.empty((ticks, n), np.float32)
+    apre, apost = np.empty(n, np.float32), np.empty(n, np.float32)
+    last = np.empty(n, np.int32)
+    st = fn(n, _ptr(w0, ctypes.c_float), _ptr(wmax, ctypes.c_float), max_ltp, ltp_tau, max_ltd, ltd_tau, dt, ticks,
+            _ptr(pre, ctypes.c_uint8), _ptr(post, ctypes.c_uint8), _ptr(traj, ctypes.c_float),
+            _ptr(apre, ctypes.c_float), _ptr(apost, ctypes.c_float), _ptr(last, ctypes.c_int))
+    if st != 0:
+        raise ValueError("reference STDP driver rejected the schedule")
+    return traj, apre, apost, last
+
+
 def _lib(prec: int):
     with _LOCK:
         if prec in _LIBS:
