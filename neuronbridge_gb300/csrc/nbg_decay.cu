@@ -13,20 +13,22 @@
 
 namespace {
 
-// tab[(r * 2 + w) * len + k] = expf(-((float)k * dt) * inv[r * 2 + w])
+// Factor w (0: LTP trace, 1: LTD trace) of rule r at gap k, the two traces of
+// one gap side by side (the engine reads both with one 8-byte load):
+// tab[(r * len + k) * 2 + w] = expf(-((float)k * dt) * inv[r * 2 + w])
 __global__ void k_decay_table(float *__restrict__ tab, const float *__restrict__ inv, int len, float dt,
                               long long total) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
     const int row = (int)(i / len), k = (int)(i % len);
     const float delta_time = (float)k * dt;
-    tab[i] = expf(-delta_time * inv[row]);
+    tab[((size_t)(row >> 1) * len + k) * 2 + (row & 1)] = expf(-delta_time * inv[row]);
 }
 
 } // namespace
 
-// Fill `tab` (device, rows x len) from the per-row inverse time constants
-// `inv_host`; synchronous.
+// Fill `tab` (device, rows x len floats, rows = 2 per rule, laid out as above)
+// from the per-row inverse time constants `inv_host`; synchronous.
 NBG_HIDDEN cudaError_t nbg_device_decay_table(float *tab, const float *inv_host, int rows, int len, float dt) {
     float *inv = nullptr;
     cudaError_t e = cudaMalloc(&inv, rows * sizeof(float));

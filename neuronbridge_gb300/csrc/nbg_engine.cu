@@ -98,6 +98,23 @@ struct LayerDev {
     float alpha;                // DENSE LIF: dt / tau
 };
 
+// Synapse records, in CSC order.  A plastic network keeps every field an
+// arrival touches in one 32-byte record -- one DRAM sector per arrival, read
+// by two 16-byte loads and written back by one -- instead of one sector in
+// each of six arrays.  A static network keeps weight and meta in 8 bytes.
+//   meta: bit 0 synapse type (1 = subtract), bits 1..7 learning rule + 1
+struct alignas(32) SynRec {
+    float w, apre, apost; // weight, the pre- and post-synaptic traces
+    int last;             // step of the last trace update
+    unsigned int meta;
+    float wmax;           // upper weight bound of the rule's clamp
+    unsigned int pad[2];
+};
+struct alignas(8) SynStatic {
+    float w;
+    unsigned int meta;
+};
+
 struct NetDev {
     int N, D, Wt, n_layers, semantics;
     float dt;
@@ -107,18 +124,21 @@ struct NetDev {
     float *v, *u, *gexc, *ginh, *iext;
     int *last;
     const int *csc_ptr, *woff;
-    float *w;
-    const float *wmax;
-    const unsigned char *meta; // bit0 type, bits1..7 rule+1
-    float *apre, *apost;
-    int *slast;
-    const float *dtab; // [rule][2][dtab_len]
+    // synapses in CSC order: SynRec (plastic networks) or SynStatic (static
+    // ones); exactly one of the two is set
+    SynRec *rec;
+    SynStatic *wst;
+    const float2 *dtab; // [rule][dtab_len] {LTP factor, LTD factor} per step gap
     int dtab_len;
     const float *rule_a; // [rule][2] = max_ltp, max_ltd
     unsigned int *mask;
     unsigned int *wsum; // per slot: one bit per mask word, set while that word is non-zero
     int Ws;             // summary words per slot (ceil(Wt / 32) + 1 padding word)
     const int *out_ptr;
+    // out lists (CSR by source): packed (mask bit << out_dbits | delay -
+    // out_dmin) when that fits 32 bits, else bit and delay in two arrays
+    const unsigned int *out_pk;
+    int out_dbits, out_dmin;
     const unsigned int *out_bit;
     const unsigned short *out_delay;
     // in-synapses from generator layers, per target, sorted by CSC rank
@@ -249,7 +269,7 @@ struct Spec {
         return (kModels != 0u && (kModels & (kModels - 1u)) == 0u) ? __builtin_ctz(kModels) : -1;
     }
     __device__ static int model(int m) { return single() >= 0 ? single() : m; }
-    __device__ static bool plastic(const NetDev &n) { return kPlastic < 0 ? n.apre != nullptr : kPlastic > 0; }
+    __device__ static bool plastic(const NetDev &n) { return kPlastic < 0 ? n.rec != nullptr : kPlastic > 0; }
 };
 constexpr unsigned kAllModels = 0x3fu;
 using GenericSpec = Spec<kAllModels, -1>;
@@ -260,87 +280,116 @@ __device__ __forceinline__ float clamp_w(float w, float wmax) {
     return w;
 }
 
-// Pair STDP (L/LearningRule/src/Rule/STDP.cpp:19-61, State/STDP_State.cpp:
-// 17-26): decay both traces from the host table by the integer step gap, then
-// the pre (Apre += 1, w -= A- Apost) or post (Apost += 1, w += A+ Apre) jump
-// and the clamp to [0, wmax].  Up to K synapses of one step with their loads
-// batched: the
-// state loads of all K are issued together, then the decay-table loads, so a
-// batch costs two memory round trips instead of two per synapse.  Entries
-// with meta < 2 (no rule) are skipped.  Same arithmetic as stdp_update.
-template <bool kPre, int K>
-__device__ __forceinline__ void stdp_batch(const NetDev &n, const int (&s)[K], const unsigned char (&meta)[K],
-                                           const float (&w0)[K], int t) {
-    int last[K];
-    float apre[K], apost[K], wmax[K], fp[K], fm[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        if (meta[k] >= 2) {
-            last[k] = n.slast[s[k]];
-            apre[k] = n.apre[s[k]];
-            apost[k] = n.apost[s[k]];
-            wmax[k] = n.wmax[s[k]];
-        }
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        fp[k] = 0.0f;
-        fm[k] = 0.0f;
-        if (meta[k] >= 2) {
-            const int rule = (int)(meta[k] >> 1) - 1;
-            const int gap = t - last[k];
-            if (gap < n.dtab_len) {
-                fp[k] = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + gap]);
-                fm[k] = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + gap]);
-            }
-        }
+// One synapse as loaded for an arrival or a post-synaptic pass.
+struct Syn {
+    float w, apre, apost, wmax;
+    int last;
+    unsigned int meta;
+};
+
+// Load synapse s: the whole 32-byte record of a plastic network (two 16-byte
+// loads of one sector, issued together), or the 8-byte static record.
+template <class S>
+__device__ __forceinline__ Syn load_syn(const NetDev &n, int s) {
+    Syn y;
+    if (S::plastic(n)) {
+        const uint4 a = reinterpret_cast<const uint4 *>(n.rec + s)[0];
+        const uint4 b = reinterpret_cast<const uint4 *>(n.rec + s)[1];
+        y.w = __uint_as_float(a.x);
+        y.apre = __uint_as_float(a.y);
+        y.apost = __uint_as_float(a.z);
+        y.last = (int)a.w;
+        y.meta = b.x;
+        y.wmax = __uint_as_float(b.y);
+    } else {
+        const uint2 a = reinterpret_cast<const uint2 *>(n.wst)[s];
+        y.w = __uint_as_float(a.x);
+        y.meta = a.y;
+        y.apre = y.apost = y.wmax = 0.0f;
+        y.last = 0;
     }
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        if (meta[k] >= 2) {
-            const int rule = (int)(meta[k] >> 1) - 1;
-            const float a = __ldg(&n.rule_a[rule * 2 + (kPre ? 1 : 0)]);
-            float xpre = apre[k] * fp[k], xpost = apost[k] * fm[k], w = w0[k];
-            if (kPre) {
-                xpre = xpre + 1.0f;
-                w = clamp_w(w + (-a * xpost), wmax[k]);
-            } else {
-                xpost = xpost + 1.0f;
-                w = clamp_w(w + a * xpre, wmax[k]);
-            }
-            n.apre[s[k]] = xpre;
-            n.apost[s[k]] = xpost;
-            n.slast[s[k]] = t;
-            n.w[s[k]] = w;
-        }
+    return y;
 }
 
-// Arrivals of one target are applied one at a time (a wider batch raises the
-// update kernel's register count past its occupancy target); the rarer
-// post-synaptic pass batches kPostChunk synapses per lane.
+// Bring synapse s's record into L2 ahead of its load (no register, no wait).
+template <class S>
+__device__ __forceinline__ void prefetch_syn(const NetDev &n, int s) {
+    const void *p = S::plastic(n) ? (const void *)(n.rec + s) : (const void *)(n.wst + s);
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+
+// Decay factors {LTP, LTD} of rule `rule` for a gap of `gap` steps; gaps past
+// the table decay to 0 (the table runs until expf underflows).
+__device__ __forceinline__ float2 decay_pair(const NetDev &n, int rule, int gap) {
+    return gap < n.dtab_len ? n.dtab[(size_t)rule * n.dtab_len + gap] : make_float2(0.0f, 0.0f);
+}
+
+// Pair STDP (L/LearningRule/src/Rule/STDP.cpp:19-61, State/STDP_State.cpp:
+// 17-26): decay both traces from the host table by the integer step gap
+// (STDP_State::SetUpdate), then the pre (Apre += 1, w -= A- Apost) or post
+// (Apost += 1, w += A+ Apre) jump and the clamp to [0, wmax]; the updated
+// weight, traces and step go back as one 16-byte store.
+template <bool kPre>
+__device__ __forceinline__ void stdp_apply(const NetDev &n, int s, const Syn &y, float2 f, float a, int t) {
+    float xpre = y.apre * f.x, xpost = y.apost * f.y, w = y.w;
+    if (kPre) {
+        xpre = xpre + 1.0f;
+        w = clamp_w(w + (-a * xpost), y.wmax);
+    } else {
+        xpost = xpost + 1.0f;
+        w = clamp_w(w + a * xpre, y.wmax);
+    }
+    reinterpret_cast<uint4 *>(n.rec + s)[0] =
+        make_uint4(__float_as_uint(w), __float_as_uint(xpre), __float_as_uint(xpost), (unsigned int)t);
+}
+
+__device__ __forceinline__ int rule_of(unsigned int meta) { return (int)((meta >> 1) & 0x7fu) - 1; }
+
+// Synapses per lane per round of a post-synaptic pass: every lane loads the
+// records of kPostChunk synapses, then their decay factors, then stores, so
+// a pass over up to 32 * kPostChunk in-synapses costs two memory round trips.
 constexpr int kPostChunk = 2;
 
 // This lane's share of a post-synaptic STDP pass over in-synapses
 // [s, s1) of a spiking neuron, striding by the warp size.
-__device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t);
+template <class S>
+__device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t) {
+    for (; s < s1; s += 32 * kPostChunk) {
+        Syn y[kPostChunk];
+        float2 f[kPostChunk];
+        float a[kPostChunk];
+#pragma unroll
+        for (int k = 0; k < kPostChunk; ++k) {
+            const int sk = s + 32 * k;
+            if (sk < s1) y[k] = load_syn<S>(n, sk);
+            else y[k].meta = 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kPostChunk; ++k) {
+            f[k] = make_float2(0.0f, 0.0f);
+            a[k] = 0.0f;
+            if (y[k].meta >= 2u) {
+                const int rule = rule_of(y[k].meta);
+                f[k] = decay_pair(n, rule, t - y[k].last);
+                a[k] = __ldg(&n.rule_a[rule * 2 + 0]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPostChunk; ++k)
+            if (y[k].meta >= 2u) stdp_apply<false>(n, s + 32 * k, y[k], f[k], a[k], t);
+    }
+}
 
 // Apply one arrival on synapse s of a target: its ProcessSpike with the
 // weight as it is before this step's pre hook, then the pre hook if the
-// synapse is plastic.  The STDP state is loaded speculatively together with
-// meta and weight (one memory round trip), then the decay-table entry.
+// synapse is plastic.  The record is one load (one sector); the decay
+// factors of its gap, one 8-byte load, follow.
 template <class S>
 __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
                                               float &acc_b, bool gate, int s, int t) {
-    const unsigned char meta = n.meta[s];
-    const float w = n.w[s];
-    int last = 0;
-    float apre = 0.0f, apost = 0.0f, wmax = 0.0f;
-    if (S::plastic(n)) { // the network has plastic synapses: state arrays exist for every synapse
-        last = n.slast[s];
-        apre = n.apre[s];
-        apost = n.apost[s];
-        wmax = n.wmax[s];
-    }
-    const int type = meta & 1;
+    const Syn y = load_syn<S>(n, s);
+    const float w = y.w;
+    const int type = y.meta & 1u;
     switch (S::model(M.model)) {
     case NBG_MODEL_LIF_VJ:
         if constexpr (S::has(NBG_MODEL_LIF_VJ)) {
@@ -381,20 +430,10 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, N
             atomicOr(n.err, kErrEventLog);
         }
     }
-    if (S::plastic(n) && meta >= 2) { // pre-synaptic pair STDP (STDP::ApplyPreSynaticSpike)
-        const int rule = (int)(meta >> 1) - 1;
-        const int gap = t - last;
-        float fp = 0.0f, fm = 0.0f;
-        if (gap < n.dtab_len) {
-            fp = __ldg(&n.dtab[(size_t)(rule * 2 + 0) * n.dtab_len + gap]);
-            fm = __ldg(&n.dtab[(size_t)(rule * 2 + 1) * n.dtab_len + gap]);
-        }
-        const float a = __ldg(&n.rule_a[rule * 2 + 1]);
-        const float xpre = apre * fp + 1.0f, xpost = apost * fm;
-        n.apre[s] = xpre;
-        n.apost[s] = xpost;
-        n.slast[s] = t;
-        n.w[s] = clamp_w(w + (-a * xpost), wmax);
+    if (S::plastic(n) && y.meta >= 2u) { // pre-synaptic pair STDP (STDP::ApplyPreSynaticSpike)
+        const int rule = rule_of(y.meta);
+        const float2 f = decay_pair(n, rule, t - y.last);
+        stdp_apply<true>(n, s, y, f, __ldg(&n.rule_a[rule * 2 + 1]), t);
     }
 }
 
@@ -404,21 +443,6 @@ template <class S>
 __device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
                                            float &acc_b, bool gate, unsigned int word, int first, int t) {
     for (; word; word &= word - 1u) apply_arrival<S>(n, M, r, acc_a, acc_b, gate, first + __ffs(word) - 1, t);
-}
-
-__device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t) {
-    for (; s < s1; s += 32 * kPostChunk) {
-        int ss[kPostChunk];
-        unsigned char mt[kPostChunk];
-        float w0[kPostChunk];
-#pragma unroll
-        for (int k = 0; k < kPostChunk; ++k) {
-            ss[k] = s + 32 * k;
-            mt[k] = ss[k] < s1 ? n.meta[ss[k]] : 0;
-            w0[k] = mt[k] >= 2 ? n.w[ss[k]] : 0.0f;
-        }
-        stdp_batch<false, kPostChunk>(n, ss, mt, w0, t);
-    }
 }
 
 // One neuron update; returns true on a spike.  `noise` is
@@ -573,12 +597,9 @@ struct GenIn {
 
 // Advance every neuron B steps (drain arrivals, integrate, compact spikes,
 // post-synaptic STDP).  One thread per neuron; all lanes stay in the loop so
-// the per-step warp collectives are full-warp.
-//   * the first kPrefetch mask words of step b+1 are loaded while step b runs
-//     (every mark for the block's slots was made by earlier launches);
-//   * the post-synaptic STDP pass of a spiking neuron is spread over its warp:
-//     the 32 lanes stride over that neuron's CSC list.
-constexpr int kPrefetch = 4; // mask words per neuron prefetched one step ahead
+// the per-step warp collectives are full-warp.  The post-synaptic STDP pass
+// of a spiking neuron is spread over its warp: the 32 lanes stride over that
+// neuron's CSC list.
 
 // x mod D for x < 2D: ring slots are advanced by adding and wrapping once
 // instead of an integer division per step and per mark (every step and
@@ -612,6 +633,18 @@ __device__ __forceinline__ void summary_clear_range(unsigned int *srow, int woff
     }
 }
 
+// Out-synapse q of the CSR by source: its mask bit and delay.
+__device__ __forceinline__ void out_entry(const NetDev &n, int q, unsigned int &bit, unsigned int &dl) {
+    if (n.out_pk) {
+        const unsigned int pk = n.out_pk[q];
+        bit = pk >> n.out_dbits;
+        dl = (pk & ((1u << n.out_dbits) - 1u)) + (unsigned int)n.out_dmin;
+    } else {
+        bit = n.out_bit[q];
+        dl = n.out_delay[q];
+    }
+}
+
 // Mark the out-synapses [q0, q1) of a spike at step t (the calling lanes
 // stride over them): bit of the synapse in slot (t + delay) % D and the
 // summary bit of its word.  No return values are used, so the atomics are
@@ -619,8 +652,9 @@ __device__ __forceinline__ void summary_clear_range(unsigned int *srow, int woff
 __device__ __forceinline__ void mark_out(const NetDev &n, int q, int q1, unsigned int t) {
 #pragma unroll 4
     for (; q < q1; q += 32) {
-        const unsigned int bit = n.out_bit[q];
-        const unsigned int slot = (t + n.out_delay[q]) % (unsigned int)n.D;
+        unsigned int bit, dl;
+        out_entry(n, q, bit, dl);
+        const unsigned int slot = (t + dl) % (unsigned int)n.D;
         const unsigned int wd = bit >> 5;
         atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
         atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
@@ -766,22 +800,25 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     const unsigned int nkey = noisy ? noise_key(n.seed, j) : 0u;
     // Fast path (in-degree <= 1024, <= 32 generator inputs): the L2-resident
     // word summary says which of this neuron's mask words hold arrivals, so
-    // only those words are loaded from HBM.  Two-stage prefetch: the summary
-    // bits of step b+2 and the flagged first kPrefetch mask words of step b+1
-    // are requested while step b runs (every mark for the block's slots was
-    // made by earlier launches, so both are final).
+    // only those words are loaded.  A pipeline three steps deep keeps the
+    // memory latency off the step: at the top of step b the summary bits of
+    // step b + 3 and the first flagged mask word of step b + 2 are requested,
+    // and the synapse records of the first arrivals of step b + 1 (whose word
+    // arrived during step b - 1) are prefetched into L2, so that when step
+    // b + 1 applies them its record loads hit L2.  Every mark for the
+    // block's slots was made by earlier launches, so all of these are final.
+    // Further flagged words of a step (rare) are loaded when it runs.
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
     const unsigned int D = (unsigned int)n.D;
     const unsigned int slot0 = (unsigned int)T0 % D; // the block's first slot; later ones by wrap_slot
-    unsigned int sb_cur = 0u, sb_nxt = 0u;
-    unsigned int w_cur[kPrefetch] = {0u, 0u, 0u, 0u};
+    // summary bits of steps b, b+1, b+2 and the first flagged word of b, b+1
+    unsigned int sbA = 0u, sbB = 0u, sbC = 0u, fwA = 0u, fwB = 0u;
     if (active && fast && nw > 0) {
-        sb_cur = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
-        if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
-        const unsigned int *r0 = n.mask + (size_t)slot0 * n.Wt + woff;
-#pragma unroll
-        for (int k = 0; k < kPrefetch; ++k)
-            if ((sb_cur >> k) & 1u) w_cur[k] = r0[k];
+        sbA = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
+        if (B > 1) sbB = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
+        if (B > 2) sbC = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw);
+        if (sbA) fwA = n.mask[(size_t)slot0 * n.Wt + woff + __ffs(sbA) - 1];
+        if (sbB) fwB = n.mask[(size_t)wrap_slot(slot0 + 1u, D) * n.Wt + woff + __ffs(sbB) - 1];
     }
     unsigned long long delivered = 0;
     unsigned int spk_steps = 0u; // bit b: this neuron spiked at step T0 + b
@@ -794,19 +831,23 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             float acc_a = 0.0f, acc_b = 0.0f;
             const bool gate = r.last > L.ip;
             if (fast) {
-                const unsigned int sb = sb_cur;
-                unsigned int wc[kPrefetch];
-#pragma unroll
-                for (int k = 0; k < kPrefetch; ++k) wc[k] = w_cur[k];
-                // prefetch: flagged words of step b+1, summary of step b+2
-                if (b + 1 < B) {
-                    const unsigned int *rn = n.mask + (size_t)wrap_slot(slot + 1u, D) * n.Wt + woff;
-#pragma unroll
-                    for (int k = 0; k < kPrefetch; ++k) w_cur[k] = ((sb_nxt >> k) & 1u) ? rn[k] : 0u;
-                    sb_cur = sb_nxt;
-                    sb_nxt = (b + 2 < B && nw > 0)
-                                 ? summary_bits(n.wsum + (size_t)wrap_slot(slot + 2u, D) * n.Ws, woff, nw)
-                                 : 0u;
+                const unsigned int sb = sbA, fw = fwA;
+                {
+                    unsigned int fwC = 0u, sbD = 0u;
+                    if (b + 2 < B && sbC)
+                        fwC = n.mask[(size_t)wrap_slot(slot + 2u, D) * n.Wt + woff + __ffs(sbC) - 1];
+                    if (b + 3 < B && nw > 0) sbD = summary_bits(n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff, nw);
+                    if (fwB) { // the records of step b + 1's first two arrivals into L2
+                        const int p0 = base + (__ffs(sbB) - 1) * 32;
+                        const unsigned int rest = fwB & (fwB - 1u);
+                        prefetch_syn<S>(n, p0 + __ffs(fwB) - 1);
+                        if (rest) prefetch_syn<S>(n, p0 + __ffs(rest) - 1);
+                    }
+                    sbA = sbB;
+                    fwA = fwB;
+                    sbB = sbC;
+                    fwB = fwC;
+                    sbC = sbD;
                 }
                 // generator arrivals of this step (pure functions of source and time)
                 unsigned int gfired = 0u, gwords = 0u;
@@ -825,19 +866,13 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                     }
                 unsigned int need = sb | gwords;
                 if (sb) summary_clear(n.wsum + (size_t)slot * n.Ws, woff, sb);
+                const int wfirst = __ffs(sb) - 1; // the word already loaded (fw), -1 if none
                 while (need) {
                     const int wi = __ffs(need) - 1;
                     need &= need - 1u;
                     unsigned int word = 0u;
                     if ((sb >> wi) & 1u) {
-                        if (wi < kPrefetch) {
-                            word = wc[0];
-#pragma unroll
-                            for (int k = 1; k < kPrefetch; ++k)
-                                if (wi == k) word = wc[k];
-                        } else {
-                            word = mrow[wi];
-                        }
+                        word = wi == wfirst ? fw : mrow[wi];
                         mrow[wi] = 0u;
                     }
                     for (unsigned int gf = gfired; gf; gf &= gf - 1u) {
@@ -874,7 +909,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             const int l = __ffs(sbal) - 1;
             sbal &= sbal - 1u;
             const int s0 = __shfl_sync(0xffffffffu, base, l), s1 = __shfl_sync(0xffffffffu, end, l);
-            post_stdp_lane(n, s0 + lane, s1, t);
+            post_stdp_lane<S>(n, s0 + lane, s1, t);
         }
         __syncwarp(); // the owners read these synapses at their next arrivals
     }
@@ -914,24 +949,52 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             }
         }
     }
-    // Propagation: the warp strides over each spiking lane's out-synapses,
-    // loading each synapse once and marking it for every step it spiked in.
-    unsigned int pbal = __ballot_sync(0xffffffffu, spk_steps != 0u);
-    while (pbal) {
-        const int l = __ffs(pbal) - 1;
-        pbal &= pbal - 1u;
-        const int jl = __shfl_sync(0xffffffffu, j, l);
-        const unsigned int steps = __shfl_sync(0xffffffffu, spk_steps, l);
-        const int q1 = n.out_ptr[jl + 1];
-#pragma unroll 2
-        for (int q = n.out_ptr[jl] + lane; q < q1; q += 32) {
-            const unsigned int bit = n.out_bit[q];
-            const unsigned int dl = n.out_delay[q];
-            const unsigned int wd = bit >> 5;
-            for (unsigned int m = steps; m; m &= m - 1u) {
-                const unsigned int slot = wrap_slot(slot0 + (unsigned int)(__ffs(m) - 1) + dl, D);
-                atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
-                atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+    // Propagation: the out-lists of all the warp's spiking lanes form one
+    // range that the 32 lanes stride over together (entry e belongs to the
+    // first lane whose inclusive prefix of list lengths exceeds e).  The
+    // list bounds of every spiking lane come in one round trip, and the
+    // entry loads of four rounds are issued before their marks.  Each
+    // synapse is loaded once and marked for every step its source spiked in.
+    {
+        int q0 = 0, cnt = 0;
+        if (spk_steps) {
+            q0 = n.out_ptr[j];
+            cnt = n.out_ptr[j + 1] - q0;
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        constexpr int kRounds = 4;
+        for (int e0 = 0; e0 < total; e0 += 32 * kRounds) {
+            unsigned int bit[kRounds], dl[kRounds], steps[kRounds];
+#pragma unroll
+            for (int k = 0; k < kRounds; ++k) {
+                const int e = e0 + 32 * k + lane;
+                int owner = 0; // first lane with incl > e (binary search over the warp's prefix)
+#pragma unroll
+                for (int w = 16; w > 0; w >>= 1) {
+                    const int c = __shfl_sync(0xffffffffu, incl, owner + w - 1);
+                    if (c <= e) owner += w;
+                }
+                const int oq = __shfl_sync(0xffffffffu, q0, owner & 31);
+                const int oe = __shfl_sync(0xffffffffu, incl - cnt, owner & 31);
+                steps[k] = __shfl_sync(0xffffffffu, spk_steps, owner & 31);
+                bit[k] = dl[k] = 0u;
+                if (e < total) out_entry(n, oq + (e - oe), bit[k], dl[k]);
+                else steps[k] = 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < kRounds; ++k) {
+                const unsigned int wd = bit[k] >> 5;
+                for (unsigned int m = steps[k]; m; m &= m - 1u) {
+                    const unsigned int slot = wrap_slot(slot0 + (unsigned int)(__ffs(m) - 1) + dl[k], D);
+                    atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit[k] & 31u));
+                    atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+                }
             }
         }
     }
@@ -1007,14 +1070,17 @@ struct nbg_engine {
     std::vector<float> init_w;
     // device buffers
     DevBuf<unsigned short> pop;
-    DevBuf<unsigned char> meta;
     DevBuf<LayerDev> d_layers;
-    DevBuf<float> v, u, gexc, ginh, iext, w, wmax, apre, apost, dtab, rule_a, trace, ev_w;
+    DevBuf<SynRec> rec;    // plastic network: synapse records
+    DevBuf<SynStatic> wst; // static network: weight + meta
+    DevBuf<float> init_w_d; // weights reset returns to, CSC order
+    DevBuf<float> v, u, gexc, ginh, iext, rule_a, trace, ev_w;
+    DevBuf<float2> dtab;
     DevBuf<int> gen_ptr, gen_pos, gen_src;
     DevBuf<unsigned short> gen_delay;
-    DevBuf<int> last, csc_ptr_d, woff, slast, out_ptr, out_ids, out_t, err, run_t0,
-        trace_slot, ev_t, ev_pos;
-    DevBuf<unsigned int> mask, wsum, out_bit;
+    DevBuf<int> last, csc_ptr_d, woff, out_ptr, out_ids, out_t, err, run_t0, trace_slot, ev_t, ev_pos;
+    DevBuf<unsigned int> mask, wsum, out_bit, out_pk;
+    int out_dbits = 0, out_dmin = 0;
     int Ws = 1;
     DevBuf<unsigned short> out_delay;
     DevBuf<unsigned int> cursor;
@@ -1087,12 +1153,8 @@ struct nbg_engine {
         n.last = last.p;
         n.csc_ptr = csc_ptr_d.p;
         n.woff = woff.p;
-        n.w = w.p;
-        n.wmax = wmax.p;
-        n.meta = meta.p;
-        n.apre = apre.p;
-        n.apost = apost.p;
-        n.slast = slast.p;
+        n.rec = rec.p;
+        n.wst = wst.p;
         n.dtab = dtab.p;
         n.dtab_len = dtab_len;
         n.rule_a = rule_a.p;
@@ -1100,6 +1162,9 @@ struct nbg_engine {
         n.wsum = wsum.p;
         n.Ws = Ws;
         n.out_ptr = out_ptr.p;
+        n.out_pk = out_pk.p;
+        n.out_dbits = out_dbits;
+        n.out_dmin = out_dmin;
         n.out_bit = out_bit.p;
         n.out_delay = out_delay.p;
         n.gen_ptr = gen_ptr.p;
@@ -1152,14 +1217,15 @@ nbg_status dense_decay_table(nbg_engine *e) {
         }
     }
     if (len > ((int64_t)1 << 24)) return fail(NBG_ERR_UNSUPPORTED, "STDP decay table would exceed 2^24 entries");
-    NBG_CUDA(e->dtab.alloc((size_t)e->n_rules * 2 * len));
-    NBG_CUDA(nbg_device_decay_table(e->dtab.p, inv.data(), e->n_rules * 2, (int)len, e->dt));
+    NBG_CUDA(e->dtab.alloc((size_t)e->n_rules * len));
+    NBG_CUDA(nbg_device_decay_table(reinterpret_cast<float *>(e->dtab.p), inv.data(), e->n_rules * 2, (int)len,
+                                    e->dt));
     e->dtab_len = (int)len;
     e->dtab_complete = true;
-    for (int row = 0; row < e->n_rules * 2; ++row) { // verify the underflow to 0
-        float last = 1.0f;
-        NBG_CUDA(cudaMemcpy(&last, e->dtab.p + (size_t)row * len + len - 1, sizeof(float), cudaMemcpyDeviceToHost));
-        if (last != 0.0f) e->dtab_complete = false;
+    for (int r = 0; r < e->n_rules; ++r) { // verify the underflow to 0
+        float2 last = make_float2(1.0f, 1.0f);
+        NBG_CUDA(cudaMemcpy(&last, e->dtab.p + (size_t)r * len + len - 1, sizeof(float2), cudaMemcpyDeviceToHost));
+        if (last.x != 0.0f || last.y != 0.0f) e->dtab_complete = false;
     }
     if (!e->dtab_complete) return fail(NBG_ERR_UNSUPPORTED, "dense STDP decay table did not reach 0");
     return NBG_OK;
@@ -1185,7 +1251,7 @@ nbg_status ensure_decay_table(nbg_engine *e, int64_t needed) {
     int64_t len = std::max<int64_t>({needed, (int64_t)4096, 2 * (int64_t)e->dtab_len});
     if (full <= ((int64_t)1 << 22)) len = std::max(len, full);
     len = std::min<int64_t>(len, (int64_t)1 << 24);
-    std::vector<float> tab((size_t)e->n_rules * 2 * len);
+    std::vector<float2> tab((size_t)e->n_rules * len);
     bool complete = true;
     for (int r = 0; r < e->n_rules; ++r) {
         const float inv_p = (float)(1.0 / (double)e->rules[r].ltp_tau);
@@ -1195,8 +1261,7 @@ nbg_status ensure_decay_table(nbg_engine *e, int64_t needed) {
             const float dtime = (float)k * e->dt;
             const float vp = std::exp(-dtime * inv_p);
             const float vm = std::exp(-dtime * inv_m);
-            tab[(size_t)(r * 2 + 0) * len + k] = vp;
-            tab[(size_t)(r * 2 + 1) * len + k] = vm;
+            tab[(size_t)r * len + k] = make_float2(vp, vm);
             if (k == len - 1) {
                 zp = vp == 0.0f;
                 zm = vm == 0.0f;
@@ -1209,6 +1274,32 @@ nbg_status ensure_decay_table(nbg_engine *e, int64_t needed) {
     e->dtab_len = (int)len;
     e->dtab_complete = complete;
     return NBG_OK;
+}
+
+// Weights from `w` (CSC order); with `traces`, also Apre = Apost = 0 and
+// last = 0.  meta and wmax are left as they are.
+__global__ void k_set_synapses(SynRec *rec, SynStatic *wst, const float *__restrict__ w, long long S, int traces) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= S) return;
+    if (rec) {
+        if (traces) {
+            reinterpret_cast<uint4 *>(rec + p)[0] = make_uint4(__float_as_uint(w[p]), 0u, 0u, 0u);
+        } else {
+            rec[p].w = w[p];
+        }
+    } else {
+        wst[p].w = w[p];
+    }
+}
+
+// Every synapse's weight back to init_w_d (and, with `traces`, its STDP state
+// to zero), on the engine's stream, synchronously.
+cudaError_t reset_synapses(nbg_engine *e, bool traces) {
+    const long long S = e->S;
+    k_set_synapses<<<(unsigned)((S + 255) / 256), 256, 0, e->stream>>>(e->rec.p, e->wst.p, e->init_w_d.p, S,
+                                                                       traces ? 1 : 0);
+    const cudaError_t ce = cudaGetLastError();
+    return ce != cudaSuccess ? ce : cudaStreamSynchronize(e->stream);
 }
 
 nbg_status upload_layers(nbg_engine *e) {
@@ -1226,14 +1317,7 @@ nbg_status reset_state(nbg_engine *e) {
     NBG_CUDA(e->ginh.zero());
     std::vector<int> last0((size_t)e->N, 10000);
     NBG_CUDA(cudaMemcpy(e->last.p, last0.data(), e->N * sizeof(int), cudaMemcpyHostToDevice));
-    if (e->S > 0) {
-        NBG_CUDA(cudaMemcpy(e->w.p, e->init_w.data(), e->S * sizeof(float), cudaMemcpyHostToDevice));
-        if (e->plastic) {
-            NBG_CUDA(e->apre.zero());
-            NBG_CUDA(e->apost.zero());
-            NBG_CUDA(e->slast.zero());
-        }
-    }
+    if (e->S > 0) NBG_CUDA(reset_synapses(e, true));
     NBG_CUDA(e->mask.zero());
     NBG_CUDA(e->wsum.zero());
     NBG_CUDA(e->err.zero());
@@ -1805,19 +1889,34 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     // inside a block aliases a slot the block drains
     e->D = e->dmax + std::min(e->dmin, kMaxBlockSteps);
     e->pop_host = pop;
-    std::vector<float> w((size_t)S), wmax((size_t)S);
-    std::vector<unsigned char> meta((size_t)S);
+    std::vector<float> w((size_t)S);
     std::vector<int> src_of((size_t)S);
     for (int64_t p = 0; p < S; ++p) {
         const int64_t s = e->csc_orig[p];
         w[p] = d->weight[s];
-        wmax[p] = d->max_weight[s];
-        meta[p] = (unsigned char)((d->type[s] & 1) | ((d->rule[s] + 1) << 1));
         src_of[p] = d->source[s];
     }
     e->init_w = w;
     e->plastic = false;
     for (int64_t s = 0; s < S && !e->plastic; ++s) e->plastic = d->rule[s] >= 0;
+    // synapse records: 32 bytes with the STDP state when anything learns
+    std::vector<SynRec> recs;
+    std::vector<SynStatic> wsts;
+    if (e->plastic) recs.resize((size_t)S);
+    else wsts.resize((size_t)S);
+    for (int64_t p = 0; p < S; ++p) {
+        const int64_t s = e->csc_orig[p];
+        const unsigned int meta = (unsigned int)((d->type[s] & 1) | ((d->rule[s] + 1) << 1));
+        if (e->plastic) {
+            SynRec &r = recs[(size_t)p];
+            r = SynRec{};
+            r.w = w[p];
+            r.meta = meta;
+            r.wmax = d->max_weight[s];
+        } else {
+            wsts[(size_t)p] = SynStatic{w[p], meta};
+        }
+    }
 
     // ---- current synapses: latch slots by target (CSC order), out-lists by source
     {
@@ -1891,6 +1990,25 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
             }
     }
     if ((uint64_t)e->Wt * 32ull > 0xFFFFFFFFull) return bail(fail(NBG_ERR_UNSUPPORTED, "too many synapses"));
+    // one 32-bit word per out-synapse when the mask bit and the delay above
+    // dmin fit in it together (one load per out-synapse instead of two)
+    std::vector<unsigned int> opk;
+    {
+        auto bits_for = [](uint64_t maxval) {
+            int b = 0;
+            while (b < 64 && (maxval >> b) != 0) ++b;
+            return b;
+        };
+        const int dbits = bits_for((uint64_t)(e->dmax - std::min(e->dmin, e->dmax)));
+        const int bbits = bits_for((uint64_t)e->Wt * 32ull - 1ull);
+        if (!obit.empty() && dbits + bbits <= 32) {
+            e->out_dbits = dbits;
+            e->out_dmin = e->dmin;
+            opk.resize(obit.size());
+            for (size_t q = 0; q < obit.size(); ++q)
+                opk[q] = (obit[q] << dbits) | (unsigned int)(odelay[q] - e->dmin);
+        }
+    }
 
     {   // update-kernel instance: the models the update threads meet (generator
         // layers have their own threads) and whether anything learns
@@ -1932,7 +2050,6 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     if (const char *rf = std::getenv("NBG_RASTER_ORDER_FAIL")) e->raster_order_fail = std::atoi(rf) != 0;
 
     chk(e->pop.upload(pop), "pop");
-    chk(e->meta.upload(meta), "meta");
     const size_t N = (size_t)e->N;
     chk(e->v.alloc(N), "v");
     chk(e->u.alloc(N), "u");
@@ -1942,19 +2059,19 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(e->last.alloc(N), "last");
     chk(e->csc_ptr_d.upload(cptr), "csc_ptr");
     chk(e->woff.upload(woff), "woff");
-    chk(e->w.alloc((size_t)S), "w");
-    if (e->plastic) { // STDP state and weight bounds only when some synapse learns
-        chk(e->wmax.upload(wmax), "wmax");
-        chk(e->apre.alloc((size_t)S), "apre");
-        chk(e->apost.alloc((size_t)S), "apost");
-        chk(e->slast.alloc((size_t)S), "slast");
-    }
+    if (e->plastic) chk(e->rec.upload(recs), "synapse records");
+    else chk(e->wst.upload(wsts), "synapse records");
+    chk(e->init_w_d.upload(w), "initial weights");
     chk(e->mask.alloc((size_t)e->D * e->Wt), "mask ring");
     e->Ws = (e->Wt + 31) / 32 + 1;
     chk(e->wsum.alloc((size_t)e->D * e->Ws), "mask summary ring");
     chk(e->out_ptr.upload(optr), "out_ptr");
-    chk(e->out_bit.upload(obit), "out_bit");
-    chk(e->out_delay.upload(odelay), "out_delay");
+    if (!opk.empty()) {
+        chk(e->out_pk.upload(opk), "out lists");
+    } else {
+        chk(e->out_bit.upload(obit), "out_bit");
+        chk(e->out_delay.upload(odelay), "out_delay");
+    }
     chk(e->gen_ptr.upload(gptr), "gen_ptr");
     chk(e->gen_pos.upload(gpos), "gen_pos");
     chk(e->gen_src.upload(gsrc), "gen_src");
@@ -2431,8 +2548,10 @@ nbg_status nbg_get_decay_table(nbg_engine *e, int rule, int which, int64_t capac
     if (out && capacity > 0) {
         NBG_CUDA(cudaSetDevice(e->device));
         const int64_t n = std::min<int64_t>(capacity, e->dtab_len);
-        NBG_CUDA(cudaMemcpy(out, e->dtab.p + (size_t)(rule * 2 + which) * e->dtab_len, n * sizeof(float),
+        std::vector<float2> row((size_t)n);
+        NBG_CUDA(cudaMemcpy(row.data(), e->dtab.p + (size_t)rule * e->dtab_len, n * sizeof(float2),
                             cudaMemcpyDeviceToHost));
+        for (int64_t k = 0; k < n; ++k) out[k] = which ? row[(size_t)k].y : row[(size_t)k].x;
     }
     return NBG_OK;
 }
@@ -2460,25 +2579,26 @@ nbg_status nbg_get_weights(nbg_engine *e, float *w, float *apre, float *apost, i
     NBG_CUDA(cudaStreamSynchronize(e->stream));
     const size_t S = (size_t)e->S;
     if (S == 0) return NBG_OK;
-    std::vector<float> tmp(S);
-    std::vector<int> itmp;
-    float *dst[3] = {w, apre, apost};
-    float *srcs[3] = {e->w.p, e->apre.p, e->apost.p};
-    for (int k = 0; k < 3; ++k) {
-        if (!dst[k]) continue;
-        if (!srcs[k]) { // no plastic synapse: traces are identically zero
-            for (size_t p = 0; p < S; ++p) dst[k][p] = 0.0f;
-            continue;
+    if (e->plastic) {
+        std::vector<SynRec> r(S);
+        NBG_CUDA(cudaMemcpy(r.data(), e->rec.p, S * sizeof(SynRec), cudaMemcpyDeviceToHost));
+        for (size_t p = 0; p < S; ++p) {
+            const int64_t o = e->csc_orig[p];
+            if (w) w[o] = r[p].w;
+            if (apre) apre[o] = r[p].apre;
+            if (apost) apost[o] = r[p].apost;
+            if (last) last[o] = r[p].last;
         }
-        NBG_CUDA(cudaMemcpy(tmp.data(), srcs[k], S * sizeof(float), cudaMemcpyDeviceToHost));
-        for (size_t p = 0; p < S; ++p) dst[k][e->csc_orig[p]] = tmp[p];
+        return NBG_OK;
     }
-    if (last && !e->plastic) {
-        for (size_t p = 0; p < S; ++p) last[p] = 0;
-    } else if (last) {
-        itmp.resize(S);
-        NBG_CUDA(cudaMemcpy(itmp.data(), e->slast.p, S * sizeof(int), cudaMemcpyDeviceToHost));
-        for (size_t p = 0; p < S; ++p) last[e->csc_orig[p]] = itmp[p];
+    std::vector<SynStatic> r(S); // no plastic synapse: traces are identically zero
+    NBG_CUDA(cudaMemcpy(r.data(), e->wst.p, S * sizeof(SynStatic), cudaMemcpyDeviceToHost));
+    for (size_t p = 0; p < S; ++p) {
+        const int64_t o = e->csc_orig[p];
+        if (w) w[o] = r[p].w;
+        if (apre) apre[o] = 0.0f;
+        if (apost) apost[o] = 0.0f;
+        if (last) last[o] = 0;
     }
     return NBG_OK;
 }
@@ -2490,7 +2610,9 @@ nbg_status nbg_set_weight(nbg_engine *e, int64_t conn, float w) {
     NBG_CUDA(cudaSetDevice(e->device));
     NBG_CUDA(cudaStreamSynchronize(e->stream));
     const int64_t p = e->orig_pos[conn];
-    NBG_CUDA(cudaMemcpy(e->w.p + p, &w, sizeof(float), cudaMemcpyHostToDevice));
+    float *dst = e->plastic ? &e->rec.p[p].w : &e->wst.p[p].w;
+    NBG_CUDA(cudaMemcpy(dst, &w, sizeof(float), cudaMemcpyHostToDevice));
+    NBG_CUDA(cudaMemcpy(e->init_w_d.p + p, &w, sizeof(float), cudaMemcpyHostToDevice));
     e->init_w[p] = w;
     return NBG_OK;
 }
@@ -2502,7 +2624,10 @@ nbg_status nbg_set_weights(nbg_engine *e, const float *w) {
     NBG_CUDA(cudaSetDevice(e->device));
     NBG_CUDA(cudaStreamSynchronize(e->stream));
     for (int64_t s = 0; s < e->S; ++s) e->init_w[e->orig_pos[s]] = w[s];
-    if (e->S > 0) NBG_CUDA(cudaMemcpy(e->w.p, e->init_w.data(), e->S * sizeof(float), cudaMemcpyHostToDevice));
+    if (e->S > 0) {
+        NBG_CUDA(cudaMemcpy(e->init_w_d.p, e->init_w.data(), e->S * sizeof(float), cudaMemcpyHostToDevice));
+        NBG_CUDA(reset_synapses(e, false)); // weights only: the STDP traces stay
+    }
     return NBG_OK;
 }
 
