@@ -68,6 +68,18 @@ nbg_status nbg_lif_forward_segment_sparse(const float *xi, const float *w_rec, i
                                           float *vprev_rec, float *z, const float *c, const float *alpha,
                                           const float *theta, const nbg_lif_grad_params *p, int L, int B, int N,
                                           void *stream);
+/* nbg_lif_forward_segment_sparse with the input term as a gather too: x is
+ * L x B x C (the segment's inputs), w_in C x N; at each step row b's input
+ * current starts from the sum, in ascending channel order, of x_t[b][c] *
+ * w_in[c] over its nonzero inputs, then adds the recurrent rows.  With spike
+ * inputs (x in {0, 1}) this is a gather-sum like the recurrent one, and no
+ * L x B x N product of the inputs is formed.  The lists live in shared
+ * memory, (2N + 2C) * 4 bytes; larger sizes than 200 KiB are rejected. */
+nbg_status nbg_lif_forward_segment_gather(const float *x, const float *w_in, int C, const float *w_rec, int32_t *spk,
+                                          int32_t *cnt, float *v, int32_t *ref, float *s_out, float *s_last,
+                                          float *u_rec, uint8_t *m_rec, float *vprev_rec, float *z, const float *c,
+                                          const float *alpha, const float *theta, const nbg_lif_grad_params *p,
+                                          int L, int B, int N, void *stream);
 nbg_status nbg_spike_lists(const float *s, int32_t *spk, int32_t *cnt, int B, int N, void *stream);
 
 /* One adjoint step (reverse time).  g_ext may be NULL (last step). */
@@ -98,6 +110,24 @@ nbg_status nbg_lif_adjoint_step_split(const float *g_parts, int n_parts, const f
                                       const nbg_lif_grad_params *p, int B, int N, void *stream);
 nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *dI_hi, const void *dI_lo,
                                 float *g_parts, int split, int B, int N, int *err, void *stream);
+
+/* One adjoint step t in one launch, N >= 512 (a multiple of 128), B = 128:
+ * the recurrent term dI_{t+1} W_rec^T on the tensor cores (as
+ * nbg_adjoint_rec_grad, from dI_hi_in / dI_lo_in) and the step of
+ * nbg_lif_adjoint_step_split on it, which writes dI_t (FP32 into dI, the
+ * split BF16 operand into dI_hi_out / dI_lo_out; the in and out operand
+ * buffers must differ).  The split-K partials never leave the chip: the 8
+ * CTAs of a cluster that share a 128-row tile reduce them through
+ * distributed shared memory, in the same order as the two-launch form, so
+ * the results are identical to it.  A bounded wait that gives up sets
+ * kUmmaTimeout (4) in *err and the step's results are invalid.  No
+ * counterpart in the reference (the reference has no adjoint). */
+nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const void *dI_hi_in, const void *dI_lo_in,
+                                      void *dI_hi_out, void *dI_lo_out, const float *g_read, float c_t,
+                                      const float *u, const float *s, const uint8_t *m, const float *vprev,
+                                      float *lam_v, float *dI, float *g_theta, float *g_alpha, const float *alpha,
+                                      const float *theta, const nbg_lif_grad_params *p, int B, int N, int *err,
+                                      void *stream);
 
 /* The recurrent weight gradient of a checkpoint segment on the tensor cores,
  * dW_rec += sum over its L steps of S_{t-1}^T dI_t, in three calls:

@@ -7,14 +7,15 @@ the network state every ``checkpoint`` steps, and the backward replays each
 segment from its checkpoint (recording u_t, s_t, m_t, v_{t-1}) and runs the
 fused adjoint kernel in reverse time.
 
-* x W_in (a whole segment at once), the adjoint's recurrent term
-  dI_{t+1} W_rec^T (per step) and the weight gradients (one product per
-  segment) are cuBLAS GEMMs through torch.
-* The forward recurrent input s_{t-1} W_rec: with binary spikes (spiking
-  mode) one fused kernel per step sums the W_rec rows of the previous step's
-  spikes (ascending order), runs the neuron update and writes the new spike
-  list; with sigmoid spikes it is a GEMM followed by the fused elementwise
-  step.
+* Spiking mode: the forward (and the backward's replay) runs each checkpoint
+  segment in one launch per row block: the input current of a step is the
+  sum of the W_in rows of the row's nonzero inputs (x_t times the row) and
+  the W_rec rows of its previous spikes, each in ascending order, so there
+  is no GEMM in the forward at all.  The adjoint's recurrent term
+  dI_{t+1} W_rec^T and the weight gradients run on tcgen05 in split BF16
+  (nbg_adjoint_tc.cu) where the shapes allow, else cuBLAS FP32.
+* Smoothed (sigmoid) mode, the finite-difference test mode: x W_in and
+  s_{t-1} W_rec are cuBLAS FP32 GEMMs followed by the fused elementwise step.
 * All elementwise work of an adjoint step is one fused kernel.
 
 Readout: y_t = a_out y_{t-1} + s_t W_out, a_out = exp(-dt / tau_out), and
@@ -50,12 +51,16 @@ _SIG = {
     "nbg_lif_forward_step_sparse": (ctypes.c_int, [_vp] * 13 + [ctypes.c_float, _vp, _vp, ctypes.POINTER(GradParams),
                                                                 ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_spike_lists": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "nbg_lif_forward_segment_gather": (ctypes.c_int, [_vp, _vp, ctypes.c_int] + [_vp] * 14 +
+                                       [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_lif_forward_segment_sparse": (ctypes.c_int, [_vp] * 15 + [ctypes.POINTER(GradParams), ctypes.c_int,
                                                                   ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_adjoint_rec_prepare": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),
     "nbg_lif_adjoint_step_split": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_float] + [_vp] * 12 +
                                    [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_adjoint_rec_grad": (ctypes.c_int, [_vp] * 5 + [ctypes.c_int] * 3 + [_vp, _vp]),
+    "nbg_lif_adjoint_step_fused": (ctypes.c_int, [_vp] * 7 + [ctypes.c_float] + [_vp] * 10 +
+                                   [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "nbg_adjoint_blocked_t": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     "nbg_adjoint_wgrad": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
                                          ctypes.c_int, _vp, _vp]),
@@ -119,6 +124,16 @@ class _SpikeLists:
             _ptr(s_out), _ptr(s_last), _ptr(u_rec), _ptr(m_rec), _ptr(vp_rec), _ptr(z), _ptr(c), _ptr(alpha),
             _ptr(theta), ctypes.byref(p), L, B, N, st))
 
+    def segment_gather(self, lib, x, w_in, w_rec, v, ref, s_out, s_last, u_rec, m_rec, vp_rec, z, c, alpha, theta,
+                       p, L, B, N, st):
+        """As segment, with the input term x_t W_in gathered over each row's
+        nonzero inputs inside the same launch (nbg_lif_forward_segment_gather)."""
+        C = x.shape[-1]
+        _lib.check(lib.nbg_lif_forward_segment_gather(
+            _ptr(x), _ptr(w_in), C, _ptr(w_rec), _ptr(self.idx[self.cur]), _ptr(self.cnt[self.cur]), _ptr(v),
+            _ptr(ref), _ptr(s_out), _ptr(s_last), _ptr(u_rec), _ptr(m_rec), _ptr(vp_rec), _ptr(z), _ptr(c),
+            _ptr(alpha), _ptr(theta), ctypes.byref(p), L, B, N, st))
+
     def step(self, lib, xi, w_rec, v, ref, s_out, u_rec, m_rec, vp_rec, z, c, alpha, theta, p, B, N, st):
         a, b = self.cur, self.cur ^ 1
         _lib.check(lib.nbg_lif_forward_step_sparse(
@@ -161,6 +176,17 @@ def _tc_ok(p, B: int, N: int) -> bool:
     return not p.smooth and B == 128 and N % 128 == 0
 
 
+# With N >= 512 the product and the adjoint step that consumes it are one
+# launch per step (nbg_lif_adjoint_step_fused: an 8-CTA cluster per 128-row
+# tile reduces its split-K partials through distributed shared memory); the
+# same sums in the same order as the two-launch form.
+FUSED_STEP = True
+
+
+def _fused_ok(p, B: int, N: int) -> bool:
+    return FUSED_STEP and _tc_ok(p, B, N) and N >= 512
+
+
 def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out):
     """Forward recurrence into caller-owned buffers: the checkpoints
     ck_*[segment] (state entering each K-step segment), the readout
@@ -186,12 +212,12 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
         ck_v[seg].copy_(v)
         ck_ref[seg].copy_(ref)
         ck_s[seg].copy_(s_prev)
-        xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
-        if sparse:  # the whole segment in one launch
+        if sparse:  # the whole segment in one launch, inputs gathered in it
             s_prev = sbuf[seg & 1]
-            lists.segment(lib, xi, w_rec, v, ref, None, s_prev, None, None, None, z, coef_dev[t0:t1], alpha, theta,
-                          p, t1 - t0, B, N, st)
+            lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, None, s_prev, None, None, None, z,
+                                 coef_dev[t0:t1], alpha, theta, p, t1 - t0, B, N, st)
             continue
+        xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
         for t in range(t0, t1):
             s = sbuf[t & 1]
             torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
@@ -229,13 +255,16 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     sparse = _sparse_ok(p, N)
     lists = _SpikeLists(B, N, x.device) if sparse else None
     tc = _tc_ok(p, B, N)
+    fused = _fused_ok(p, B, N)
     if tc:
         w_hi = torch.empty(N * N, device=x.device, dtype=torch.bfloat16)
         w_lo = torch.empty(N * N, device=x.device, dtype=torch.bfloat16)
-        d_hi = torch.empty(B * N, device=x.device, dtype=torch.bfloat16)
-        d_lo = torch.empty(B * N, device=x.device, dtype=torch.bfloat16)
+        # the split BF16 operand dI: two buffers in the fused form (a step
+        # reads one while writing the other), else one
+        d_hi = [torch.empty(B * N, device=x.device, dtype=torch.bfloat16) for _ in range(2 if fused else 1)]
+        d_lo = [torch.empty(B * N, device=x.device, dtype=torch.bfloat16) for _ in range(2 if fused else 1)]
         split = min(TC_SPLIT, N // 64)
-        g_parts = torch.empty((split, B, N), device=x.device, dtype=torch.float32)
+        g_parts = None if fused else torch.empty((split, B, N), device=x.device, dtype=torch.float32)
         tc_err = torch.zeros(1, device=x.device, dtype=torch.int32)
         _lib.check(lib.nbg_adjoint_rec_prepare(_ptr(w_rec), _ptr(w_hi), _ptr(w_lo), N, st))
     tc_w = tc and N % 256 == 0
@@ -256,11 +285,12 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         L = t1 - t0
         v, ref = ck_v[seg].clone(), ck_ref[seg].clone()
         S[0].copy_(ck_s[seg])
-        xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
         if sparse:  # replay the segment in one launch, recording u, m, v_{t-1} and s
             lists.load(lib, S[0], B, N, st)
-            lists.segment(lib, xi, w_rec, v, ref, S[1], None, U, M, VP, None, None, alpha, theta, p, L, B, N, st)
+            lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, S[1], None, U, M, VP, None, None, alpha, theta,
+                                 p, L, B, N, st)
         else:
+            xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
             for k in range(L):
                 torch.addmm(xi[k], S[k], w_rec, out=I)
                 _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
@@ -268,13 +298,28 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                                                     ctypes.byref(p), B, N, st))
         for k in reversed(range(L)):
             t = t0 + k
+            if fused:  # dI_{t+1} W_rec^T and the step t that consumes it, one launch
+                cur, nxt = t & 1, (t + 1) & 1
+                if have_next:
+                    _lib.check(lib.nbg_lif_adjoint_step_fused(
+                        _ptr(w_hi), _ptr(w_lo), _ptr(d_hi[nxt]), _ptr(d_lo[nxt]), _ptr(d_hi[cur]), _ptr(d_lo[cur]),
+                        _ptr(g_read), float(coef[t]), _ptr(U[k]), _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]),
+                        _ptr(lam_v), _ptr(dI[k]), _ptr(g_theta), _ptr(g_alpha), _ptr(alpha), _ptr(theta),
+                        ctypes.byref(p), B, N, _ptr(tc_err), st))
+                else:  # the last step of the run: no recurrent term yet
+                    _lib.check(lib.nbg_lif_adjoint_step_split(
+                        None, split, _ptr(g_read), float(coef[t]), _ptr(U[k]), _ptr(S[k + 1]), _ptr(M[k]),
+                        _ptr(VP[k]), _ptr(lam_v), _ptr(dI[k]), _ptr(d_hi[cur]), _ptr(d_lo[cur]), _ptr(g_theta),
+                        _ptr(g_alpha), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
+                have_next = True
+                continue
             if tc:  # g_parts holds dI_{t+1} W_rec^T from the previous iteration
                 _lib.check(lib.nbg_lif_adjoint_step_split(
                     _ptr(g_parts) if have_next else None, split, _ptr(g_read), float(coef[t]), _ptr(U[k]),
-                    _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]), _ptr(lam_v), _ptr(dI[k]), _ptr(d_hi), _ptr(d_lo),
+                    _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]), _ptr(lam_v), _ptr(dI[k]), _ptr(d_hi[0]), _ptr(d_lo[0]),
                     _ptr(g_theta), _ptr(g_alpha), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
-                _lib.check(lib.nbg_adjoint_rec_grad(_ptr(w_hi), _ptr(w_lo), _ptr(d_hi), _ptr(d_lo), _ptr(g_parts),
-                                                    split, B, N, _ptr(tc_err), st))
+                _lib.check(lib.nbg_adjoint_rec_grad(_ptr(w_hi), _ptr(w_lo), _ptr(d_hi[0]), _ptr(d_lo[0]),
+                                                    _ptr(g_parts), split, B, N, _ptr(tc_err), st))
                 have_next = True
                 continue
             ge = None

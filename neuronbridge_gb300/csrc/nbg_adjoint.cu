@@ -150,15 +150,27 @@ __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_sparse(
 // so each CTA runs its row through all L steps with v and ref in registers
 // and the spike list in shared memory: no launch per step and no exchange
 // between CTAs.  The arithmetic is k_lif_fwd_sparse's, in the same order.
+//
+// kGather: the input term too is a gather instead of a precomputed xi.  At
+// every step the CTA lists row b's nonzero inputs x_t[b][c] (ascending c,
+// with their values) in shared memory and starts the sum from them:
+// I_t = (sum over listed c of x_t[b][c] * W_in[c]) + (the W_rec rows of the
+// previous step's spikes), each term added in ascending order.  With spike
+// inputs (x in {0, 1}) the products are exact and the step costs a few rows
+// of W_in instead of a GEMM of the segment's inputs.
+template <bool kGather>
 __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_segment(
-    const float *__restrict__ xi, const float *__restrict__ w, int *__restrict__ spk, int *__restrict__ cnt,
+    const float *__restrict__ xi, const float *__restrict__ x, const float *__restrict__ w_in, int C,
+    const float *__restrict__ w, int *__restrict__ spk, int *__restrict__ cnt,
     float *__restrict__ v, int *__restrict__ ref, float *__restrict__ s_out, float *__restrict__ s_last,
     float *__restrict__ u_rec, unsigned char *__restrict__ m_rec, float *__restrict__ vprev_rec,
     float *__restrict__ z, const float *__restrict__ c, const float *__restrict__ alpha,
     const float *__restrict__ theta, nbg_lif_grad_params p, int L, int B, int N) {
-    extern __shared__ int seg_lists[]; // [2][N]
+    extern __shared__ int seg_lists[]; // [2][N], then (kGather) in_idx[C], in_val[C]
     __shared__ int warp_base[kSparseThreads / 32 + 1];
     __shared__ int list_cnt[2];
+    int *in_idx = seg_lists + 2 * N;
+    float *in_val = reinterpret_cast<float *>(in_idx + C);
     const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const size_t row = (size_t)b * N, plane = (size_t)B * N;
     const int nq = (N + kSparseThreads - 1) / kSparseThreads;
@@ -181,12 +193,54 @@ __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_segment(
     __syncthreads();
     int cur = 0;
     for (int step = 0; step < L; ++step) {
-        const float *xs = xi + (size_t)step * plane + row;
         float acc[kSparseCols];
+        if constexpr (kGather) {
+            // row b's nonzero inputs of this step, ascending
+            const float *xr = x + ((size_t)step * B + b) * C;
+            int nin = 0;
+            for (int c0 = 0; c0 < C; c0 += kSparseThreads) {
+                const int ch = c0 + tid;
+                const float xv = ch < C ? xr[ch] : 0.0f;
+                const bool nz = xv != 0.0f;
+                const unsigned bal = __ballot_sync(0xffffffffu, nz);
+                if (lane == 0) warp_base[wid] = __popc(bal);
+                __syncthreads();
+                if (tid == 0) {
+                    int sum = 0;
+                    for (int k = 0; k < kSparseThreads / 32; ++k) {
+                        const int cc = warp_base[k];
+                        warp_base[k] = sum;
+                        sum += cc;
+                    }
+                    warp_base[kSparseThreads / 32] = sum;
+                }
+                __syncthreads();
+                if (nz) {
+                    const int at = nin + warp_base[wid] + __popc(bal & ((1u << lane) - 1u));
+                    in_idx[at] = ch;
+                    in_val[at] = xv;
+                }
+                nin += warp_base[kSparseThreads / 32];
+                __syncthreads();
+            }
 #pragma unroll
-        for (int q = 0; q < kSparseCols; ++q) {
-            const int j = tid + q * kSparseThreads;
-            acc[q] = (q < nq && j < N) ? xs[j] : 0.0f;
+            for (int q = 0; q < kSparseCols; ++q) acc[q] = 0.0f;
+            for (int k = 0; k < nin; ++k) {
+                const float xv = in_val[k];
+                const float *wr = w_in + (size_t)in_idx[k] * N;
+#pragma unroll
+                for (int q = 0; q < kSparseCols; ++q) {
+                    const int j = tid + q * kSparseThreads;
+                    if (q < nq && j < N) acc[q] = acc[q] + xv * __ldg(&wr[j]);
+                }
+            }
+        } else {
+            const float *xs = xi + (size_t)step * plane + row;
+#pragma unroll
+            for (int q = 0; q < kSparseCols; ++q) {
+                const int j = tid + q * kSparseThreads;
+                acc[q] = (q < nq && j < N) ? xs[j] : 0.0f;
+            }
         }
         const int *list = seg_lists + cur * N;
         const int nl = list_cnt[cur];
@@ -364,8 +418,33 @@ nbg_status nbg_lif_forward_segment_sparse(const float *xi, const float *w_rec, i
     if (N > kSparseThreads * kSparseCols)
         return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step supports up to %d neurons",
                         kSparseThreads * kSparseCols);
-    k_lif_fwd_segment<<<B, kSparseThreads, 2 * N * sizeof(int), (cudaStream_t)stream>>>(
-        xi, w_rec, spk, cnt, v, ref, s_out, s_last, u_rec, m_rec, vprev_rec, z, c, alpha, theta, *p, L, B, N);
+    k_lif_fwd_segment<false><<<B, kSparseThreads, 2 * N * sizeof(int), (cudaStream_t)stream>>>(
+        xi, nullptr, nullptr, 0, w_rec, spk, cnt, v, ref, s_out, s_last, u_rec, m_rec, vprev_rec, z, c, alpha,
+        theta, *p, L, B, N);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_lif_forward_segment_gather(const float *x, const float *w_in, int C, const float *w_rec, int32_t *spk,
+                                          int32_t *cnt, float *v, int32_t *ref, float *s_out, float *s_last,
+                                          float *u_rec, uint8_t *m_rec, float *vprev_rec, float *z, const float *c,
+                                          const float *alpha, const float *theta, const nbg_lif_grad_params *p,
+                                          int L, int B, int N, void *stream) {
+    if (!x || !w_in || C <= 0 || !w_rec || !spk || !cnt || !v || !ref || !alpha || !theta || !p || (z && !c) ||
+        L <= 0 || B <= 0 || N <= 0)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_forward_segment_gather: bad arguments");
+    if (p->smooth) return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step needs binary spikes (smooth = 0)");
+    if (N > kSparseThreads * kSparseCols)
+        return nbg_fail(NBG_ERR_UNSUPPORTED, "the spike-driven step supports up to %d neurons",
+                        kSparseThreads * kSparseCols);
+    const size_t smem = (2 * (size_t)N + 2 * (size_t)C) * sizeof(int);
+    if (smem > 200 * 1024) return nbg_fail(NBG_ERR_UNSUPPORTED, "too many inputs for the gather form (C = %d)", C);
+    if (smem > 48 * 1024)
+        NBG_CUDA(cudaFuncSetAttribute(k_lif_fwd_segment<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    k_lif_fwd_segment<true><<<B, kSparseThreads, smem, (cudaStream_t)stream>>>(
+        nullptr, x, w_in, C, w_rec, spk, cnt, v, ref, s_out, s_last, u_rec, m_rec, vprev_rec, z, c, alpha, theta,
+        *p, L, B, N);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

@@ -235,6 +235,190 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// One adjoint step in one launch: the recurrent product of step t + 1 and
+// the adjoint step t that consumes it.  Grid (N / 128, kAdjCluster) in
+// clusters of kAdjCluster CTAs along y: the CTAs of a cluster split the K
+// range of one 128-row tile of W exactly as k_adj_umma's split-K does
+// (cluster rank = split index), run the same three split products into
+// TMEM, and move their 128 x 128 partial into their own shared memory (the
+// drained pipeline stages), laid out [b][i].  After a cluster barrier, rank
+// r reduces batch rows [16 r, 16 r + 16) of the tile over the partials of
+// ranks 0..7 in order (read through distributed shared memory) -- the sum
+// k_lif_adj_split forms from g_parts, so the result is the same bit for bit
+// -- and runs the adjoint step on those elements, writing dI_t in FP32 and
+// as the split BF16 operand of the next step's product into the other of
+// two buffers (the next launch reads this one while writing its own).  A
+// second cluster barrier keeps every CTA's shared memory alive until its
+// peers have read it.  Waits on mbarriers are bounded as in k_adj_umma; a
+// CTA that gives up still takes part in both cluster barriers, and the
+// error word marks the step's results invalid.
+constexpr int kAdjCluster = 8;
+
+__global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 1) k_adj_step_umma(
+    const __nv_bfloat16 *__restrict__ w_hi, const __nv_bfloat16 *__restrict__ w_lo,
+    const __nv_bfloat16 *__restrict__ d_hi_in, const __nv_bfloat16 *__restrict__ d_lo_in,
+    __nv_bfloat16 *__restrict__ d_hi_out, __nv_bfloat16 *__restrict__ d_lo_out, const float *__restrict__ g_read,
+    float c_t, const float *__restrict__ u, const float *__restrict__ s, const unsigned char *__restrict__ m,
+    const float *__restrict__ vprev, float *__restrict__ lam_v, float *__restrict__ dI, float *__restrict__ g_theta,
+    float *__restrict__ g_alpha, const float *__restrict__ alpha, const float *__restrict__ theta,
+    nbg_lif_grad_params p, int n, int *__restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(stages + kAdjStages * kAdjStageBytes);
+    uint64_t *empty = full + kAdjStages;
+    uint64_t *done = empty + kAdjStages;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *abort = (volatile int *)(tmem_slot + 1);
+    float *part = reinterpret_cast<float *>(stages); // [b][i], 64 KiB, after the pipeline has drained
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t rank;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    const int mt = blockIdx.x, ks = (int)rank;
+    const int kchunks = n / kKChunk;
+    const int per = kchunks / kAdjCluster;
+    const int kc0 = ks * per;
+    const int iters = (ks == kAdjCluster - 1) ? kchunks - kc0 : per;
+
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < kAdjStages; ++st) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], 1);
+        }
+        mbar_init(done, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(kAdjTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    // Programmatic dependent launch: W is constant during the backward, so
+    // the first stages' W tiles are requested before the wait for the
+    // previous step (which writes dI_{t+1}, lam_v and the gradients).
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (warp == 0 && lane == 0) { // producer
+        const int pre = iters < kAdjStages ? iters : kAdjStages;
+        for (int it = 0; it < pre; ++it) {
+            uint8_t *st = stages + it * kAdjStageBytes;
+            const size_t a_blk = (size_t)mt * kchunks + kc0 + it;
+            mbar_expect_tx(&full[it], kAdjStageBytes);
+            bulk_copy(st, (const uint8_t *)w_hi + a_blk * kAdjBlockA, kAdjBlockA, &full[it]);
+            bulk_copy(st + kAdjBlockA, (const uint8_t *)w_lo + a_blk * kAdjBlockA, kAdjBlockA, &full[it]);
+        }
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        for (int it = 0; it < pre; ++it) {
+            uint8_t *st = stages + it * kAdjStageBytes;
+            const int kc = kc0 + it;
+            bulk_copy(st + 2 * kAdjBlockA, (const uint8_t *)d_hi_in + (size_t)kc * kAdjBlockB, kAdjBlockB, &full[it]);
+            bulk_copy(st + 2 * kAdjBlockA + kAdjBlockB, (const uint8_t *)d_lo_in + (size_t)kc * kAdjBlockB,
+                      kAdjBlockB, &full[it]);
+        }
+        for (int it = pre; it < iters; ++it) {
+            const int st_i = it % kAdjStages;
+            if (!mbar_wait(&empty[st_i], ((it / kAdjStages) & 1) ^ 1, abort)) break;
+            uint8_t *st = stages + st_i * kAdjStageBytes;
+            const int kc = kc0 + it;
+            const size_t a_blk = (size_t)mt * kchunks + kc;
+            mbar_expect_tx(&full[st_i], kAdjStageBytes);
+            bulk_copy(st, (const uint8_t *)w_hi + a_blk * kAdjBlockA, kAdjBlockA, &full[st_i]);
+            bulk_copy(st + kAdjBlockA, (const uint8_t *)w_lo + a_blk * kAdjBlockA, kAdjBlockA, &full[st_i]);
+            bulk_copy(st + 2 * kAdjBlockA, (const uint8_t *)d_hi_in + (size_t)kc * kAdjBlockB, kAdjBlockB, &full[st_i]);
+            bulk_copy(st + 2 * kAdjBlockA + kAdjBlockB, (const uint8_t *)d_lo_in + (size_t)kc * kAdjBlockB,
+                      kAdjBlockB, &full[st_i]);
+        }
+    } else if (warp == 1 && lane == 0) { // MMA issuer
+        for (int it = 0; it < iters; ++it) {
+            const int st_i = it % kAdjStages;
+            if (!mbar_wait(&full[st_i], (it / kAdjStages) & 1, abort)) break;
+            fence_after();
+            const uint32_t a_hi = smem_addr(stages + st_i * kAdjStageBytes);
+            const uint32_t a_lo = a_hi + kAdjBlockA;
+            const uint32_t b_hi = a_hi + 2 * kAdjBlockA;
+            const uint32_t b_lo = b_hi + kAdjBlockB;
+#pragma unroll
+            for (int k = 0; k < kKChunk / 16; ++k) {
+                mma(tmem, make_desc(a_hi + 256 * k), make_desc(b_hi + 256 * k), kAdjIdesc, (it | k) != 0);
+                mma(tmem, make_desc(a_lo + 256 * k), make_desc(b_hi + 256 * k), kAdjIdesc, 1u);
+                mma(tmem, make_desc(a_hi + 256 * k), make_desc(b_lo + 256 * k), kAdjIdesc, 1u);
+            }
+            commit(&empty[st_i]);
+        }
+        commit(done);
+    }
+    __syncwarp();
+    asm volatile("griddepcontrol.wait;" ::: "memory"); // the previous step's writes are visible
+    mbar_wait(done, 0, abort);
+    __syncthreads();
+    fence_after();
+    // partial accumulator -> own shared memory, [b][i]: warp w holds rows
+    // i = 32 (w % 4) + lane and batch columns 64 (w / 4) + 16 c16 + c
+    {
+        const int q = warp & 3, h = warp >> 2;
+        const int il = 32 * q + lane;
+        if (!*abort) {
+#pragma unroll
+            for (int c16 = 0; c16 < 4; ++c16) {
+                float acc[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * h + 16 * c16), acc);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) part[(64 * h + 16 * c16 + c) * kAdjM + il] = acc[c];
+            }
+        }
+    }
+    fence_before();
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    // reduce batch rows [16 ks, 16 ks + 16) over the cluster's partials, in
+    // rank order, and run the adjoint step on them
+    {
+        const int il = threadIdx.x & 127, bsub = threadIdx.x >> 7;
+        const int i = mt * kAdjM + il;
+        const uint32_t local = smem_addr(part);
+        const float th = theta[i], al = alpha[i];
+#pragma unroll 2
+        for (int k = 0; k < 8; ++k) {
+            const int b = 16 * ks + bsub + 2 * k;
+            const uint32_t off = local + (uint32_t)((b * kAdjM + il) * 4);
+            float ge = 0.0f;
+#pragma unroll
+            for (int r = 0; r < kAdjCluster; ++r) {
+                uint32_t ra;
+                float x;
+                asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(off), "r"(r));
+                asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x) : "r"(ra) : "memory");
+                ge = r == 0 ? x : ge + x;
+            }
+            const size_t idx = (size_t)b * n + i;
+            const float uu = u[idx], ss = s[idx], lv = lam_v[idx];
+            const float dsdu = p.smooth ? p.slope * ss * (1.0f - ss) : surrogate(uu - th, p.slope);
+            float gs = c_t * g_read[idx] - lv * (uu - p.v_reset);
+            gs = gs + ge;
+            const float gu = gs * dsdu + lv * (1.0f - ss);
+            const float gm = m[idx] ? gu : 0.0f;
+            dI[idx] = gm;
+            const size_t o = blocked_index(b, i, n);
+            split_bf16(gm, d_hi_out[o], d_lo_out[o]);
+            lam_v[idx] = gm * (1.0f - al);
+            g_theta[idx] = g_theta[idx] - gs * dsdu;
+            g_alpha[idx] = g_alpha[idx] + gm * (p.v_rest - vprev[idx]);
+        }
+    }
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    if (threadIdx.x == 0 && *abort) atomicOr(err, kUmmaTimeout);
+    if (warp == 2) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kAdjTmemCols)
+                     : "memory");
+    }
+}
+
 // [L][B][R] FP32 -> the R x (L*B) matrix (row r, K = l*B + b) in the blocked
 // layout, split into hi and lo (lo may be null: the values are exact in BF16).
 __global__ void k_blocked_t(const float *__restrict__ src, int L, int B, int R, __nv_bfloat16 *__restrict__ hi,
@@ -448,6 +632,41 @@ nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *
     cfg.numAttrs = 1;
     NBG_CUDA(cudaLaunchKernelEx(&cfg, k_adj_umma, (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo,
                                 (const __nv_bfloat16 *)dI_hi, (const __nv_bfloat16 *)dI_lo, g_parts, N, split, err));
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
+
+nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const void *dI_hi_in, const void *dI_lo_in,
+                                      void *dI_hi_out, void *dI_lo_out, const float *g_read, float c_t,
+                                      const float *u, const float *s, const uint8_t *m, const float *vprev,
+                                      float *lam_v, float *dI, float *g_theta, float *g_alpha, const float *alpha,
+                                      const float *theta, const nbg_lif_grad_params *p, int B, int N, int *err,
+                                      void *stream) {
+    if (!w_hi || !w_lo || !dI_hi_in || !dI_lo_in || !dI_hi_out || !dI_lo_out || !g_read || !u || !s || !m ||
+        !vprev || !lam_v || !dI || !g_theta || !g_alpha || !alpha || !theta || !p || !err || !adj_shape_ok(B, N) ||
+        N / kKChunk < kAdjCluster || dI_hi_in == dI_hi_out || dI_lo_in == dI_lo_out)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_adjoint_step_fused: bad arguments (B must be %d, N a multiple of %d "
+                        "and at least %d, distinct in and out operand buffers)", kAdjN, kAdjM,
+                        kAdjCluster * kKChunk);
+    static bool attr_set = false;
+    if (!attr_set) {
+        NBG_CUDA(cudaFuncSetAttribute(k_adj_step_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmemBytes));
+        attr_set = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(N / kAdjM, kAdjCluster);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kAdjSmemBytes;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    NBG_CUDA(cudaLaunchKernelEx(&cfg, k_adj_step_umma, (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo,
+                                (const __nv_bfloat16 *)dI_hi_in, (const __nv_bfloat16 *)dI_lo_in,
+                                (__nv_bfloat16 *)dI_hi_out, (__nv_bfloat16 *)dI_lo_out, g_read, c_t, u, s, m, vprev,
+                                lam_v, dI, g_theta, g_alpha, alpha, theta, *p, N, err));
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

@@ -270,6 +270,12 @@ struct Spec {
     }
     __device__ static int model(int m) { return single() >= 0 ? single() : m; }
     __device__ static bool plastic(const NetDev &n) { return kPlastic < 0 ? n.rec != nullptr : kPlastic > 0; }
+    // Shape of the arrival drain.  Deep: one mask word per step, three steps
+    // ahead, for networks whose neurons receive a few arrivals per hundred
+    // steps (the current-based Izhikevich + STDP profile).  Wide: every
+    // flagged word one step ahead and arrivals loaded several at a time, for
+    // networks with arrivals at most steps (Poisson-driven static LIF).
+    static constexpr bool deep = kPlastic > 0;
 };
 constexpr unsigned kAllModels = 0x3fu;
 using GenericSpec = Spec<kAllModels, -1>;
@@ -380,14 +386,13 @@ __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, i
     }
 }
 
-// Apply one arrival on synapse s of a target: its ProcessSpike with the
-// weight as it is before this step's pre hook, then the pre hook if the
-// synapse is plastic.  The record is one load (one sector); the decay
-// factors of its gap, one 8-byte load, follow.
+// Apply one arrival on synapse s of a target, its record y already loaded:
+// its ProcessSpike with the weight as it is before this step's pre hook,
+// then the pre hook if the synapse is plastic (the decay factors of its gap,
+// one 8-byte load, then one 16-byte store).
 template <class S>
-__device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
-                                              float &acc_b, bool gate, int s, int t) {
-    const Syn y = load_syn<S>(n, s);
+__device__ __forceinline__ void apply_loaded(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                             float &acc_b, bool gate, int s, const Syn &y, int t) {
     const float w = y.w;
     const int type = y.meta & 1u;
     switch (S::model(M.model)) {
@@ -434,6 +439,55 @@ __device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, N
         const int rule = rule_of(y.meta);
         const float2 f = decay_pair(n, rule, t - y.last);
         stdp_apply<true>(n, s, y, f, __ldg(&n.rule_a[rule * 2 + 1]), t);
+    }
+}
+
+template <class S>
+__device__ __forceinline__ void apply_arrival(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                              float &acc_b, bool gate, int s, int t) {
+    apply_loaded<S>(n, M, r, acc_a, acc_b, gate, s, load_syn<S>(n, s), t);
+}
+
+// Arrivals loaded per round by the wide drain.
+constexpr int kBatch = 2;
+
+// The set bits of `word` (first = the CSC position of bit 0), in ascending
+// order, for a neuron with arrivals at most steps: the records of up to
+// kBatch arrivals are loaded before any of them is applied (distinct
+// synapses, so no load depends on an earlier apply), one memory round trip
+// per round instead of one per arrival.  The synapse at CSC position gpos
+// (the neuron's generator input in a static network, else -1) comes from
+// registers.
+template <class S>
+__device__ __forceinline__ void apply_word_batched(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                                   float &acc_b, bool gate, unsigned int word, int first, int t,
+                                                   int gpos, float gw, unsigned int gmeta) {
+    while (word) {
+        int sk[kBatch];
+        Syn y[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) {
+            sk[k] = -1;
+            if (word) {
+                sk[k] = first + __ffs(word) - 1;
+                word &= word - 1u;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) {
+            if (sk[k] < 0) continue;
+            if (sk[k] == gpos) {
+                y[k].w = gw;
+                y[k].meta = gmeta;
+                y[k].apre = y[k].apost = y[k].wmax = 0.0f;
+                y[k].last = 0;
+            } else {
+                y[k] = load_syn<S>(n, sk[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k)
+            if (sk[k] >= 0) apply_loaded<S>(n, M, r, acc_a, acc_b, gate, sk[k], y[k], t);
     }
 }
 
@@ -593,6 +647,8 @@ constexpr int kGenCached = 1;
 struct GenIn {
     int local, delay, pos;
     float prob;
+    float w;           // static networks: the synapse's weight and meta,
+    unsigned int meta; // constant within a launch, so kept in registers
 };
 
 // Advance every neuron B steps (drain arrivals, integrate, compact spikes,
@@ -757,12 +813,21 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
         gin[q].delay = 0;
         gin[q].pos = 0;
         gin[q].prob = -1.0f; // never fires
+        gin[q].w = 0.0f;
+        gin[q].meta = 0u;
         if (active && g0 + q < g1) {
             gin[q].prob = generator_prob(n, n.gen_src[g0 + q], &gin[q].local);
             gin[q].delay = n.gen_delay[g0 + q];
             gin[q].pos = n.gen_pos[g0 + q];
+            if (!S::plastic(n)) { // static weights change only between run calls
+                const uint2 a = reinterpret_cast<const uint2 *>(n.wst)[base + gin[q].pos];
+                gin[q].w = __uint_as_float(a.x);
+                gin[q].meta = a.y;
+            }
         }
     }
+    // the generator input's CSC position when its record is in registers
+    const int gen_cached_pos = (!S::plastic(n) && active && g0 < g1) ? base + gin[0].pos : -1;
     // everything below reads or writes what the previous block's launch wrote
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // external spikes of the block's steps (InputSpike::ProcessEvent): one
@@ -800,25 +865,43 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     const unsigned int nkey = noisy ? noise_key(n.seed, j) : 0u;
     // Fast path (in-degree <= 1024, <= 32 generator inputs): the L2-resident
     // word summary says which of this neuron's mask words hold arrivals, so
-    // only those words are loaded.  A pipeline three steps deep keeps the
-    // memory latency off the step: at the top of step b the summary bits of
-    // step b + 3 and the first flagged mask word of step b + 2 are requested,
-    // and the synapse records of the first arrivals of step b + 1 (whose word
-    // arrived during step b - 1) are prefetched into L2, so that when step
-    // b + 1 applies them its record loads hit L2.  Every mark for the
-    // block's slots was made by earlier launches, so all of these are final.
-    // Further flagged words of a step (rare) are loaded when it runs.
+    // only those words are loaded.  Every mark for the block's slots was made
+    // by earlier launches, so summary bits and words can be loaded early.
+    // * Deep drain (S::deep): a pipeline three steps deep keeps the memory
+    //   latency off the step.  At the top of step b the summary bits of step
+    //   b + 3 and the first flagged mask word of step b + 2 are requested,
+    //   and the synapse records of the first arrivals of step b + 1 (whose
+    //   word arrived during step b - 1) are prefetched into L2, so that step
+    //   b + 1 finds them there.  Further flagged words of a step (rare at a
+    //   few arrivals per hundred steps) are loaded when it runs.
+    // * Wide drain: the summary of step b + 2 and the first kWide flagged
+    //   words of step b + 1 are requested while step b runs, the records of
+    //   step b + 1's arrivals are prefetched into L2 at the end of step b,
+    //   and the arrivals of a word are applied kBatch per memory round trip.
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
     const unsigned int D = (unsigned int)n.D;
     const unsigned int slot0 = (unsigned int)T0 % D; // the block's first slot; later ones by wrap_slot
-    // summary bits of steps b, b+1, b+2 and the first flagged word of b, b+1
+    constexpr int kWide = 4;
+    // deep: summary bits of steps b, b+1, b+2 and the first flagged word of b, b+1
     unsigned int sbA = 0u, sbB = 0u, sbC = 0u, fwA = 0u, fwB = 0u;
+    // wide: summary bits of steps b, b+1 and the first kWide words of step b (loads in flight)
+    unsigned int sb_cur = 0u, sb_nxt = 0u;
+    unsigned int w_cur[kWide] = {0u, 0u, 0u, 0u};
     if (active && fast && nw > 0) {
-        sbA = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
-        if (B > 1) sbB = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
-        if (B > 2) sbC = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw);
-        if (sbA) fwA = n.mask[(size_t)slot0 * n.Wt + woff + __ffs(sbA) - 1];
-        if (sbB) fwB = n.mask[(size_t)wrap_slot(slot0 + 1u, D) * n.Wt + woff + __ffs(sbB) - 1];
+        if constexpr (S::deep) {
+            sbA = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
+            if (B > 1) sbB = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
+            if (B > 2) sbC = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw);
+            if (sbA) fwA = n.mask[(size_t)slot0 * n.Wt + woff + __ffs(sbA) - 1];
+            if (sbB) fwB = n.mask[(size_t)wrap_slot(slot0 + 1u, D) * n.Wt + woff + __ffs(sbB) - 1];
+        } else {
+            sb_cur = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
+            if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
+            const unsigned int *r0 = n.mask + (size_t)slot0 * n.Wt + woff;
+#pragma unroll
+            for (int k = 0; k < kWide; ++k)
+                if ((sb_cur >> k) & 1u) w_cur[k] = r0[k];
+        }
     }
     unsigned long long delivered = 0;
     unsigned int spk_steps = 0u; // bit b: this neuron spiked at step T0 + b
@@ -831,12 +914,16 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             float acc_a = 0.0f, acc_b = 0.0f;
             const bool gate = r.last > L.ip;
             if (fast) {
-                const unsigned int sb = sbA, fw = fwA;
-                {
+                unsigned int sb, fw = 0u;
+                unsigned int wc[kWide];
+                if constexpr (S::deep) {
+                    sb = sbA;
+                    fw = fwA;
                     unsigned int fwC = 0u, sbD = 0u;
                     if (b + 2 < B && sbC)
                         fwC = n.mask[(size_t)wrap_slot(slot + 2u, D) * n.Wt + woff + __ffs(sbC) - 1];
-                    if (b + 3 < B && nw > 0) sbD = summary_bits(n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff, nw);
+                    if (b + 3 < B && nw > 0)
+                        sbD = summary_bits(n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff, nw);
                     if (fwB) { // the records of step b + 1's first two arrivals into L2
                         const int p0 = base + (__ffs(sbB) - 1) * 32;
                         const unsigned int rest = fwB & (fwB - 1u);
@@ -848,6 +935,19 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                     sbB = sbC;
                     fwB = fwC;
                     sbC = sbD;
+                } else {
+                    sb = sb_cur;
+#pragma unroll
+                    for (int k = 0; k < kWide; ++k) wc[k] = w_cur[k];
+                    if (b + 1 < B) { // words of step b + 1, summary of step b + 2
+                        const unsigned int *rn = n.mask + (size_t)wrap_slot(slot + 1u, D) * n.Wt + woff;
+#pragma unroll
+                        for (int k = 0; k < kWide; ++k) w_cur[k] = ((sb_nxt >> k) & 1u) ? rn[k] : 0u;
+                        sb_cur = sb_nxt;
+                        sb_nxt = (b + 2 < B && nw > 0)
+                                     ? summary_bits(n.wsum + (size_t)wrap_slot(slot + 2u, D) * n.Ws, woff, nw)
+                                     : 0u;
+                    }
                 }
                 // generator arrivals of this step (pure functions of source and time)
                 unsigned int gfired = 0u, gwords = 0u;
@@ -866,13 +966,22 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                     }
                 unsigned int need = sb | gwords;
                 if (sb) summary_clear(n.wsum + (size_t)slot * n.Ws, woff, sb);
-                const int wfirst = __ffs(sb) - 1; // the word already loaded (fw), -1 if none
+                const int wfirst = __ffs(sb) - 1; // deep: the word already loaded (fw), -1 if none
                 while (need) {
                     const int wi = __ffs(need) - 1;
                     need &= need - 1u;
                     unsigned int word = 0u;
                     if ((sb >> wi) & 1u) {
-                        word = wi == wfirst ? fw : mrow[wi];
+                        if constexpr (S::deep) {
+                            word = wi == wfirst ? fw : mrow[wi];
+                        } else if (wi < kWide) {
+                            word = wc[0];
+#pragma unroll
+                            for (int k = 1; k < kWide; ++k)
+                                if (wi == k) word = wc[k];
+                        } else {
+                            word = mrow[wi];
+                        }
                         mrow[wi] = 0u;
                     }
                     for (unsigned int gf = gfired; gf; gf &= gf - 1u) {
@@ -881,7 +990,11 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                         if ((gp >> 5) == wi) word |= 1u << (gp & 31);
                     }
                     delivered += __popc(word);
-                    apply_word<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
+                    if constexpr (S::deep)
+                        apply_word<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
+                    else
+                        apply_word_batched<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t, gen_cached_pos,
+                                              gin[0].w, gin[0].meta);
                 }
             } else {
                 int gq = g0;
@@ -900,6 +1013,13 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             }
             spk = update_neuron<S>(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
+            if constexpr (!S::deep) {
+                if (fast && b + 1 < B) { // records of step b + 1's arrivals (its words have arrived) into L2
+#pragma unroll
+                    for (int k = 0; k < kWide; ++k)
+                        for (unsigned int m = w_cur[k]; m; m &= m - 1u) prefetch_syn<S>(n, base + k * 32 + __ffs(m) - 1);
+                }
+            }
         }
         if (spk) spk_steps |= 1u << b;
         // post-synaptic STDP (STDP::ApplyPostSynaticSpike) of every spiking

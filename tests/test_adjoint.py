@@ -238,3 +238,79 @@ def test_segment_forward_equals_per_step_launches():
     assert out[0][2].sum() > 0  # the rows spike
     for a, b in zip(out[0], out[1]):
         assert torch.equal(a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("binary", [True, False])
+def test_segment_gather_equals_ascending_input_sum(binary):
+    """nbg_lif_forward_segment_gather (the input term gathered over each row's
+    nonzero inputs inside the segment launch) equals the precomputed-input
+    segment fed xi_t = sum over c, ascending, of x_t[:, c] * W_in[c] in FP32,
+    bit for bit: spike inputs (exact products) and sparse real-valued ones,
+    with more channels than the CTA has threads."""
+    from neuronbridge_gb300.adjoint import GradParams, _bind, _SpikeLists, _stream
+
+    lib = _bind()
+    g = torch.Generator(device="cuda").manual_seed(2)
+    B, N, L, C = 32, 512, 25, 300
+    w_rec = torch.randn(N, N, device="cuda", generator=g) * 0.3
+    w_in = torch.randn(C, N, device="cuda", generator=g) * 0.5
+    x = (torch.rand(L, B, C, device="cuda", generator=g) < 0.05).float()
+    if not binary:
+        x = x * torch.rand(L, B, C, device="cuda", generator=g) * 2.0
+    xi = torch.zeros(L, B, N, device="cuda")
+    for ch in range(C):  # elementwise adds: ascending channel order, one rounding each
+        xi = xi + x[:, :, ch:ch + 1] * w_in[ch]
+    alpha = torch.full((N,), 0.05, device="cuda")
+    theta = torch.rand(N, device="cuda", generator=g) * 0.5 + 0.5
+    p = GradParams(0.0, 0.0, 10.0, 3, 0)
+    c = torch.linspace(0.1, 1.0, L, device="cuda")
+    st = _stream()
+    out = []
+    for gather in (False, True):
+        lists = _SpikeLists(B, N, "cuda")
+        v, ref = torch.zeros(B, N, device="cuda"), torch.zeros(B, N, device="cuda", dtype=torch.int32)
+        S = torch.zeros((L + 1, B, N), device="cuda")
+        U = torch.zeros((L, B, N), device="cuda")
+        z = torch.zeros((B, N), device="cuda")
+        lists.load(lib, S[0], B, N, st)
+        if gather:
+            lists.segment_gather(lib, x, w_in, w_rec, v, ref, S[1], None, U, None, None, z, c, alpha, theta, p, L,
+                                 B, N, st)
+        else:
+            lists.segment(lib, xi, w_rec, v, ref, S[1], None, U, None, None, z, c, alpha, theta, p, L, B, N, st)
+        torch.cuda.synchronize()
+        out.append((v, ref, S, U, z))
+    assert out[0][2].sum() > 0
+    for a, b in zip(out[0], out[1]):
+        assert torch.equal(a, b)
+
+
+@pytest.mark.gpu
+def test_fused_adjoint_step_equals_two_launch_form(monkeypatch):
+    """N = 512, B = 128, spiking mode: each backward step as one launch
+    (nbg_lif_adjoint_step_fused, split-K partials reduced through distributed
+    shared memory) gives the same gradients, bit for bit, as the product and
+    the step as two launches, and stays within the FP64 tolerance."""
+    from neuronbridge_gb300 import adjoint
+    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+
+    kw = dict(n_in=64, n_rec=512, n_out=5, checkpoint=20, seed=11)
+    torch.manual_seed(0)
+    model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, **kw, **SPIKING)
+    rates = torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0
+    x = poisson_inputs(rates, T, 128, dt=1.0, seed=3)
+    labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
+    assert adjoint._fused_ok(model.params, 128, 512)
+    loss_f, fused = _grads(model, x, labels)
+    monkeypatch.setattr(adjoint, "FUSED_STEP", False)
+    loss_u, unfused = _grads(model, x, labels)
+    assert loss_f == loss_u
+    for g, h in zip(fused, unfused):
+        assert torch.equal(g, h)
+    ref_params = [p.detach().double().cpu().requires_grad_(True) for p in _params(model)]
+    ref_loss = _ref_loss(model, x.double().cpu(), labels.cpu(), ref_params, False)
+    ref_loss.backward()
+    for name, g, r in zip(("w_in", "w_rec", "w_out", "alpha", "theta"), fused, ref_params):
+        scale = r.grad.abs().max().item()
+        assert (g.double().cpu() - r.grad).abs().max().item() <= 1e-3 * scale, name
