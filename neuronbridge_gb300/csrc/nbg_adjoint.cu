@@ -151,6 +151,39 @@ __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_sparse(
 // and the spike list in shared memory: no launch per step and no exchange
 // between CTAs.  The arithmetic is k_lif_fwd_sparse's, in the same order.
 //
+// acc[q] (column tid + q * kSparseThreads) += the rows idx[0..n) of w (N
+// columns), in ascending k, each scaled by val[k] when kScaled.  The rows are
+// fetched kRowBatch at a time before any is added, so a batch costs one L2
+// round trip instead of one per row; the additions keep their order.
+constexpr int kRowBatch = 4;
+template <bool kScaled>
+__device__ __forceinline__ void gather_rows(float (&acc)[kSparseCols], const float *__restrict__ w,
+                                            const int *idx, const float *val, int n, int tid, int nq, int N) {
+    for (int k0 = 0; k0 < n; k0 += kRowBatch) {
+        float x[kRowBatch][kSparseCols];
+#pragma unroll
+        for (int r = 0; r < kRowBatch; ++r) {
+            const float *wr = w + (size_t)(k0 + r < n ? idx[k0 + r] : 0) * N;
+#pragma unroll
+            for (int q = 0; q < kSparseCols; ++q) {
+                const int j = tid + q * kSparseThreads;
+                x[r][q] = (k0 + r < n && q < nq && j < N) ? __ldg(&wr[j]) : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kRowBatch; ++r) {
+            if (k0 + r >= n) break;
+            const float v = kScaled ? val[k0 + r] : 1.0f;
+#pragma unroll
+            for (int q = 0; q < kSparseCols; ++q) {
+                const int j = tid + q * kSparseThreads;
+                if (q < nq && j < N) acc[q] = kScaled ? acc[q] + v * x[r][q] : acc[q] + x[r][q];
+            }
+        }
+    }
+}
+
+//
 // kGather: the input term too is a gather instead of a precomputed xi.  At
 // every step the CTA lists row b's nonzero inputs x_t[b][c] (ascending c,
 // with their values) in shared memory and starts the sum from them:
@@ -225,15 +258,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_segment(
             }
 #pragma unroll
             for (int q = 0; q < kSparseCols; ++q) acc[q] = 0.0f;
-            for (int k = 0; k < nin; ++k) {
-                const float xv = in_val[k];
-                const float *wr = w_in + (size_t)in_idx[k] * N;
-#pragma unroll
-                for (int q = 0; q < kSparseCols; ++q) {
-                    const int j = tid + q * kSparseThreads;
-                    if (q < nq && j < N) acc[q] = acc[q] + xv * __ldg(&wr[j]);
-                }
-            }
+            gather_rows<true>(acc, w_in, in_idx, in_val, nin, tid, nq, N);
         } else {
             const float *xs = xi + (size_t)step * plane + row;
 #pragma unroll
@@ -243,15 +268,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_lif_fwd_segment(
             }
         }
         const int *list = seg_lists + cur * N;
-        const int nl = list_cnt[cur];
-        for (int k = 0; k < nl; ++k) {
-            const float *wr = w + (size_t)list[k] * N;
-#pragma unroll
-            for (int q = 0; q < kSparseCols; ++q) {
-                const int j = tid + q * kSparseThreads;
-                if (q < nq && j < N) acc[q] = acc[q] + __ldg(&wr[j]);
-            }
-        }
+        gather_rows<false>(acc, w, list, nullptr, list_cnt[cur], tid, nq, N);
         int *out_list = seg_lists + (cur ^ 1) * N;
         int base = 0;
         const float ct = z ? c[step] : 0.0f;

@@ -386,15 +386,17 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
         for (int k = 0; k < 8; ++k) {
             const int b = 16 * ks + bsub + 2 * k;
             const uint32_t off = local + (uint32_t)((b * kAdjM + il) * 4);
-            float ge = 0.0f;
+            // the eight partials are loaded back to back, then added in rank order
+            float x[kAdjCluster];
 #pragma unroll
             for (int r = 0; r < kAdjCluster; ++r) {
                 uint32_t ra;
-                float x;
                 asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(off), "r"(r));
-                asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x) : "r"(ra) : "memory");
-                ge = r == 0 ? x : ge + x;
+                asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x[r]) : "r"(ra));
             }
+            float ge = x[0];
+#pragma unroll
+            for (int r = 1; r < kAdjCluster; ++r) ge = ge + x[r];
             const size_t idx = (size_t)b * n + i;
             const float uu = u[idx], ss = s[idx], lv = lam_v[idx];
             const float dsdu = p.smooth ? p.slope * ss * (1.0f - ss) : surrogate(uu - th, p.slope);
