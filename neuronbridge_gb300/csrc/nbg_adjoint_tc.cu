@@ -355,6 +355,26 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     }
     __syncwarp();
     asm volatile("griddepcontrol.wait;" ::: "memory"); // the previous step's writes are visible
+    // this thread's share of the adjoint step: batch rows 16 ks + bsub + 2 k
+    // of column i.  Its operands are loaded now, while the products run.
+    const int il = threadIdx.x & 127, bsub = threadIdx.x >> 7;
+    const int i = mt * kAdjM + il;
+    constexpr int kRows = 8;
+    float op_u[kRows], op_s[kRows], op_lv[kRows], op_gr[kRows], op_gt[kRows], op_ga[kRows], op_vp[kRows];
+    unsigned char op_m[kRows];
+#pragma unroll
+    for (int k = 0; k < kRows; ++k) {
+        const size_t idx = (size_t)(16 * ks + bsub + 2 * k) * n + i;
+        op_u[k] = u[idx];
+        op_s[k] = s[idx];
+        op_lv[k] = lam_v[idx];
+        op_gr[k] = g_read[idx];
+        op_gt[k] = g_theta[idx];
+        op_ga[k] = g_alpha[idx];
+        op_vp[k] = vprev[idx];
+        op_m[k] = m[idx];
+    }
+    const float th = theta[i], al = alpha[i];
     mbar_wait(done, 0, abort);
     __syncthreads();
     fence_after();
@@ -378,38 +398,39 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     // reduce batch rows [16 ks, 16 ks + 16) over the cluster's partials, in
     // rank order, and run the adjoint step on them
     {
-        const int il = threadIdx.x & 127, bsub = threadIdx.x >> 7;
-        const int i = mt * kAdjM + il;
         const uint32_t local = smem_addr(part);
-        const float th = theta[i], al = alpha[i];
-#pragma unroll 2
-        for (int k = 0; k < 8; ++k) {
-            const int b = 16 * ks + bsub + 2 * k;
-            const uint32_t off = local + (uint32_t)((b * kAdjM + il) * 4);
-            // the eight partials are loaded back to back, then added in rank order
-            float x[kAdjCluster];
+        // every partial of the thread's rows, loaded back to back, then added
+        // in rank order
+        float x[kRows][kAdjCluster];
+#pragma unroll
+        for (int k = 0; k < kRows; ++k) {
+            const uint32_t off = local + (uint32_t)(((16 * ks + bsub + 2 * k) * kAdjM + il) * 4);
 #pragma unroll
             for (int r = 0; r < kAdjCluster; ++r) {
                 uint32_t ra;
                 asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(off), "r"(r));
-                asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x[r]) : "r"(ra));
+                asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x[k][r]) : "r"(ra));
             }
-            float ge = x[0];
+        }
 #pragma unroll
-            for (int r = 1; r < kAdjCluster; ++r) ge = ge + x[r];
+        for (int k = 0; k < kRows; ++k) {
+            const int b = 16 * ks + bsub + 2 * k;
+            float ge = x[k][0];
+#pragma unroll
+            for (int r = 1; r < kAdjCluster; ++r) ge = ge + x[k][r];
             const size_t idx = (size_t)b * n + i;
-            const float uu = u[idx], ss = s[idx], lv = lam_v[idx];
+            const float uu = op_u[k], ss = op_s[k], lv = op_lv[k];
             const float dsdu = p.smooth ? p.slope * ss * (1.0f - ss) : surrogate(uu - th, p.slope);
-            float gs = c_t * g_read[idx] - lv * (uu - p.v_reset);
+            float gs = c_t * op_gr[k] - lv * (uu - p.v_reset);
             gs = gs + ge;
             const float gu = gs * dsdu + lv * (1.0f - ss);
-            const float gm = m[idx] ? gu : 0.0f;
+            const float gm = op_m[k] ? gu : 0.0f;
             dI[idx] = gm;
             const size_t o = blocked_index(b, i, n);
             split_bf16(gm, d_hi_out[o], d_lo_out[o]);
             lam_v[idx] = gm * (1.0f - al);
-            g_theta[idx] = g_theta[idx] - gs * dsdu;
-            g_alpha[idx] = g_alpha[idx] + gm * (p.v_rest - vprev[idx]);
+            g_theta[idx] = op_gt[k] - gs * dsdu;
+            g_alpha[idx] = op_ga[k] + gm * (p.v_rest - op_vp[k]);
         }
     }
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");

@@ -317,11 +317,25 @@ __device__ __forceinline__ Syn load_syn(const NetDev &n, int s) {
     return y;
 }
 
-// Bring synapse s's record into L2 ahead of its load (no register, no wait).
+// Bring synapse s's record into this SM's L1 ahead of its load (no
+// register, no wait).
 template <class S>
 __device__ __forceinline__ void prefetch_syn(const NetDev &n, int s) {
     const void *p = S::plastic(n) ? (const void *)(n.rec + s) : (const void *)(n.wst + s);
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+
+// Plastic network: once synapse s's record is in L1, bring the decay
+// factors its arrival at step t will read into L1 as well (read from the
+// record now; a later change of its `last` only makes this prefetch miss).
+__device__ __forceinline__ void prefetch_decay(const NetDev &n, int s, int t) {
+    const int last = n.rec[s].last;
+    const unsigned int meta = n.rec[s].meta;
+    const int gap = t - last;
+    if (meta >= 2u && gap >= 0 && gap < n.dtab_len) {
+        const float2 *p = n.dtab + (size_t)((int)((meta >> 1) & 0x7fu) - 1) * n.dtab_len + gap;
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
+    }
 }
 
 // Decay factors {LTP, LTD} of rule `rule` for a gap of `gap` steps; gaps past
@@ -871,12 +885,13 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     //   latency off the step.  At the top of step b the summary bits of step
     //   b + 3 and the first flagged mask word of step b + 2 are requested,
     //   and the synapse records of the first arrivals of step b + 1 (whose
-    //   word arrived during step b - 1) are prefetched into L2, so that step
-    //   b + 1 finds them there.  Further flagged words of a step (rare at a
+    //   word arrived during step b - 1) are prefetched into L1; at the end of
+    //   step b the first one's decay factors follow, so that step b + 1
+    //   finds both on the SM.  Further flagged words of a step (rare at a
     //   few arrivals per hundred steps) are loaded when it runs.
     // * Wide drain: the summary of step b + 2 and the first kWide flagged
     //   words of step b + 1 are requested while step b runs, the records of
-    //   step b + 1's arrivals are prefetched into L2 at the end of step b,
+    //   step b + 1's arrivals are prefetched into L1 at the end of step b,
     //   and the arrivals of a word are applied kBatch per memory round trip.
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
     const unsigned int D = (unsigned int)n.D;
@@ -924,7 +939,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                         fwC = n.mask[(size_t)wrap_slot(slot + 2u, D) * n.Wt + woff + __ffs(sbC) - 1];
                     if (b + 3 < B && nw > 0)
                         sbD = summary_bits(n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff, nw);
-                    if (fwB) { // the records of step b + 1's first two arrivals into L2
+                    if (fwB) { // the records of step b + 1's first two arrivals into L1
                         const int p0 = base + (__ffs(sbB) - 1) * 32;
                         const unsigned int rest = fwB & (fwB - 1u);
                         prefetch_syn<S>(n, p0 + __ffs(fwB) - 1);
@@ -1013,8 +1028,12 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             }
             spk = update_neuron<S>(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
-            if constexpr (!S::deep) {
-                if (fast && b + 1 < B) { // records of step b + 1's arrivals (its words have arrived) into L2
+            if constexpr (S::deep) {
+                // the first arrival of step b + 1 (its record was prefetched at
+                // the top of this step): its decay factors into L1
+                if (fast && S::plastic(n) && fwA) prefetch_decay(n, base + (__ffs(sbA) - 1) * 32 + __ffs(fwA) - 1, t + 1);
+            } else {
+                if (fast && b + 1 < B) { // records of step b + 1's arrivals (its words have arrived) into L1
 #pragma unroll
                     for (int k = 0; k < kWide; ++k)
                         for (unsigned int m = w_cur[k]; m; m &= m - 1u) prefetch_syn<S>(n, base + k * 32 + __ffs(m) - 1);
