@@ -130,6 +130,7 @@ struct NetDev {
     SynStatic *wst;
     const float2 *dtab; // [rule][dtab_len] {LTP factor, LTD factor} per step gap
     int dtab_len;
+    int sdtab_len; // entries of rule 0's table copied into shared memory per CTA (0: none)
     const float *rule_a; // [rule][2] = max_ltp, max_ltd
     unsigned int *mask;
     unsigned int *wsum; // per slot: one bit per mask word, set while that word is non-zero
@@ -325,22 +326,17 @@ __device__ __forceinline__ void prefetch_syn(const NetDev &n, int s) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
 }
 
-// Plastic network: once synapse s's record is in L1, bring the decay
-// factors its arrival at step t will read into L1 as well (read from the
-// record now; a later change of its `last` only makes this prefetch miss).
-__device__ __forceinline__ void prefetch_decay(const NetDev &n, int s, int t) {
-    const int last = n.rec[s].last;
-    const unsigned int meta = n.rec[s].meta;
-    const int gap = t - last;
-    if (meta >= 2u && gap >= 0 && gap < n.dtab_len) {
-        const float2 *p = n.dtab + (size_t)((int)((meta >> 1) & 0x7fu) - 1) * n.dtab_len + gap;
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
-    }
-}
-
 // Decay factors {LTP, LTD} of rule `rule` for a gap of `gap` steps; gaps past
 // the table decay to 0 (the table runs until expf underflows).
+// The first entries of rule 0's decay table, copied into each CTA's shared
+// memory at the start of a launch (the table does not change within a run
+// call): most gaps are short, so most lookups leave the L2 round trip out
+// of the arrival's dependent chain.
+extern __shared__ float2 s_dtab[];
+constexpr int kSharedDecayEntries = 4096; // 32 KiB
+
 __device__ __forceinline__ float2 decay_pair(const NetDev &n, int rule, int gap) {
+    if (rule == 0 && gap < n.sdtab_len) return s_dtab[gap];
     return gap < n.dtab_len ? n.dtab[(size_t)rule * n.dtab_len + gap] : make_float2(0.0f, 0.0f);
 }
 
@@ -806,6 +802,8 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     // only what no launch writes (network structure, parameters, generator
     // inputs), overlapping this launch's tail.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    for (int k = threadIdx.x; k < n.sdtab_len; k += blockDim.x) s_dtab[k] = n.dtab[k];
+    if (n.sdtab_len) __syncthreads();
 
     Model L;
     NeuronRegs r;
@@ -885,9 +883,8 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     //   latency off the step.  At the top of step b the summary bits of step
     //   b + 3 and the first flagged mask word of step b + 2 are requested,
     //   and the synapse records of the first arrivals of step b + 1 (whose
-    //   word arrived during step b - 1) are prefetched into L1; at the end of
-    //   step b the first one's decay factors follow, so that step b + 1
-    //   finds both on the SM.  Further flagged words of a step (rare at a
+    //   word arrived during step b - 1) are prefetched into L1, so that step
+    //   b + 1 finds them on the SM.  Further flagged words of a step (rare at a
     //   few arrivals per hundred steps) are loaded when it runs.
     // * Wide drain: the summary of step b + 2 and the first kWide flagged
     //   words of step b + 1 are requested while step b runs, the records of
@@ -1028,11 +1025,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             }
             spk = update_neuron<S>(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
-            if constexpr (S::deep) {
-                // the first arrival of step b + 1 (its record was prefetched at
-                // the top of this step): its decay factors into L1
-                if (fast && S::plastic(n) && fwA) prefetch_decay(n, base + (__ffs(sbA) - 1) * 32 + __ffs(fwA) - 1, t + 1);
-            } else {
+            if constexpr (!S::deep) {
                 if (fast && b + 1 < B) { // records of step b + 1's arrivals (its words have arrived) into L1
 #pragma unroll
                     for (int k = 0; k < kWide; ++k)
@@ -1296,6 +1289,7 @@ struct nbg_engine {
         n.wst = wst.p;
         n.dtab = dtab.p;
         n.dtab_len = dtab_len;
+        n.sdtab_len = plastic && n_rules > 0 ? std::min(dtab_len, kSharedDecayEntries) : 0;
         n.rule_a = rule_a.p;
         n.mask = mask.p;
         n.wsum = wsum.p;
@@ -1505,6 +1499,7 @@ void launch_block(nbg_engine *e, const NetDev &nd, int B, int toff, int slot, bo
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(e->threads);
+    cfg.dynamicSmemBytes = (size_t)nd.sdtab_len * sizeof(float2);
     cfg.stream = e->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
