@@ -370,6 +370,9 @@ constexpr int kPostChunk = 2;
 // [s, s1) of a spiking neuron, striding by the warp size.
 template <class S>
 __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t) {
+    // every record of this lane's share into L1 first: the rounds after the
+    // first find theirs there
+    for (int q = s + 32 * kPostChunk; q < s1; q += 32) prefetch_syn<S>(n, q);
     for (; s < s1; s += 32 * kPostChunk) {
         Syn y[kPostChunk];
         float2 f[kPostChunk];
@@ -1033,7 +1036,12 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                 }
             }
         }
-        if (spk) spk_steps |= 1u << b;
+        if (spk) {
+            // the out-list bounds the propagation reads after the last step
+            if (!spk_steps)
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(n.out_ptr + j)));
+            spk_steps |= 1u << b;
+        }
         // post-synaptic STDP (STDP::ApplyPostSynaticSpike) of every spiking
         // lane, the warp striding over that neuron's in-synapses
         unsigned int sbal = S::plastic(n) ? __ballot_sync(0xffffffffu, spk && end > base) : 0u;
@@ -1056,31 +1064,18 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     // launch reads their marks (arrivals fall at or after T0 + B, and the
     // ring never aliases this block's slots), so the loads they need overlap
     // with other warps' steps instead of stalling every step.
-    // Raster: output-layer spikes, one cursor reservation per warp.
-    {
-        const int nrec = (active && L.record) ? __popc(spk_steps) : 0;
-        int incl = nrec;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total > 0) {
-            unsigned int pos = 0;
-            if (lane == 31) pos = atomicAdd(n.cursor, (unsigned int)total);
-            pos = __shfl_sync(0xffffffffu, pos, 31) + (unsigned int)(incl - nrec);
-            if (nrec > 0) {
-                if (pos + (unsigned int)nrec <= (unsigned int)n.out_cap) {
-                    for (unsigned int m = spk_steps; m; m &= m - 1u, ++pos) {
-                        n.out_ids[pos] = j;
-                        n.out_t[pos] = T0 + __ffs(m) - 1;
-                    }
-                } else {
-                    atomicOr(n.err, kErrOverflow);
-                }
-            }
-        }
+    // Raster: output-layer spikes, one cursor reservation per warp; the
+    // reservation is requested here and its result used after the
+    // propagation, so that its round trip overlaps the marks.
+    const int nrec = (active && L.record) ? __popc(spk_steps) : 0;
+    int rincl = nrec;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, rincl, o);
+        if (lane >= o) rincl += y;
     }
+    const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
+    unsigned int rpos = 0;
+    if (rtotal > 0 && lane == 31) rpos = atomicAdd(n.cursor, (unsigned int)rtotal);
     // Propagation: the out-lists of all the warp's spiking lanes form one
     // range that the 32 lanes stride over together (entry e belongs to the
     // first lane whose inclusive prefix of list lengths exceeds e).  The
@@ -1127,6 +1122,19 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                     atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit[k] & 31u));
                     atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
                 }
+            }
+        }
+    }
+    if (rtotal > 0) {
+        unsigned int pos = __shfl_sync(0xffffffffu, rpos, 31) + (unsigned int)(rincl - nrec);
+        if (nrec > 0) {
+            if (pos + (unsigned int)nrec <= (unsigned int)n.out_cap) {
+                for (unsigned int m = spk_steps; m; m &= m - 1u, ++pos) {
+                    n.out_ids[pos] = j;
+                    n.out_t[pos] = T0 + __ffs(m) - 1;
+                }
+            } else {
+                atomicOr(n.err, kErrOverflow);
             }
         }
     }
