@@ -59,7 +59,8 @@ BYTES_PER_STATIC_EVENT = 12
 BYTES_PER_POST_UPDATE = 36
 # DRAM bytes (read + write) of one k_update launch of this workload (10 steps x
 # 100k neurons) from an ncu capture of that launch with a cold L2
-KUPDATE_TRAFFIC_BYTES = 62.5e6
+# (30.24 MB read + 0.16 MB written)
+KUPDATE_TRAFFIC_BYTES = 30.39e6
 # DRAM bytes (read + write) of one k_update launch of the 256-instance batched
 # workload (15 steps), scaled from an ncu capture on its first 32 instances
 BATCHED_TRAFFIC_BYTES = 2.206e9  # 238.3 MB on 282,235 LIF neurons x 2,612,540 / 282,235
