@@ -101,14 +101,15 @@ struct LayerDev {
 // Synapse records, in CSC order.  A plastic network keeps every field an
 // arrival touches in one 32-byte record -- one DRAM sector per arrival, read
 // by two 16-byte loads and written back by one -- instead of one sector in
-// each of six arrays.  A static network keeps weight and meta in 8 bytes.
+// each of six arrays.  The rule's two jump sizes ride along in the record, so
+// an arrival has no further dependent load besides its decay factors.  A static network keeps weight and meta in 8 bytes.
 //   meta: bit 0 synapse type (1 = subtract), bits 1..7 learning rule + 1
 struct alignas(32) SynRec {
     float w, apre, apost; // weight, the pre- and post-synaptic traces
     int last;             // step of the last trace update
     unsigned int meta;
     float wmax;           // upper weight bound of the rule's clamp
-    unsigned int pad[2];
+    float a_pre, a_post;  // the rule's Max_LTD and Max_LTP (its pre and post jumps)
 };
 struct alignas(8) SynStatic {
     float w;
@@ -131,7 +132,6 @@ struct NetDev {
     const float2 *dtab; // [rule][dtab_len] {LTP factor, LTD factor} per step gap
     int dtab_len;
     int sdtab_len; // entries of rule 0's table copied into shared memory per CTA (0: none)
-    const float *rule_a; // [rule][2] = max_ltp, max_ltd
     unsigned int *mask;
     unsigned int *wsum; // per slot: one bit per mask word, set while that word is non-zero
     int Ws;             // summary words per slot (ceil(Wt / 32) + 1 padding word)
@@ -289,7 +289,7 @@ __device__ __forceinline__ float clamp_w(float w, float wmax) {
 
 // One synapse as loaded for an arrival or a post-synaptic pass.
 struct Syn {
-    float w, apre, apost, wmax;
+    float w, apre, apost, wmax, a_pre, a_post;
     int last;
     unsigned int meta;
 };
@@ -308,11 +308,13 @@ __device__ __forceinline__ Syn load_syn(const NetDev &n, int s) {
         y.last = (int)a.w;
         y.meta = b.x;
         y.wmax = __uint_as_float(b.y);
+        y.a_pre = __uint_as_float(b.z);
+        y.a_post = __uint_as_float(b.w);
     } else {
         const uint2 a = reinterpret_cast<const uint2 *>(n.wst)[s];
         y.w = __uint_as_float(a.x);
         y.meta = a.y;
-        y.apre = y.apost = y.wmax = 0.0f;
+        y.apre = y.apost = y.wmax = y.a_pre = y.a_post = 0.0f;
         y.last = 0;
     }
     return y;
@@ -390,7 +392,7 @@ __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, i
             if (y[k].meta >= 2u) {
                 const int rule = rule_of(y[k].meta);
                 f[k] = decay_pair(n, rule, t - y[k].last);
-                a[k] = __ldg(&n.rule_a[rule * 2 + 0]);
+                a[k] = y[k].a_post;
             }
         }
 #pragma unroll
@@ -451,7 +453,7 @@ __device__ __forceinline__ void apply_loaded(const NetDev &n, const Model &M, Ne
     if (S::plastic(n) && y.meta >= 2u) { // pre-synaptic pair STDP (STDP::ApplyPreSynaticSpike)
         const int rule = rule_of(y.meta);
         const float2 f = decay_pair(n, rule, t - y.last);
-        stdp_apply<true>(n, s, y, f, __ldg(&n.rule_a[rule * 2 + 1]), t);
+        stdp_apply<true>(n, s, y, f, y.a_pre, t);
     }
 }
 
@@ -492,7 +494,7 @@ __device__ __forceinline__ void apply_word_batched(const NetDev &n, const Model 
             if (sk[k] == gpos) {
                 y[k].w = gw;
                 y[k].meta = gmeta;
-                y[k].apre = y[k].apost = y[k].wmax = 0.0f;
+                y[k].apre = y[k].apost = y[k].wmax = y[k].a_pre = y[k].a_post = 0.0f;
                 y[k].last = 0;
             } else {
                 y[k] = load_syn<S>(n, sk[k]);
@@ -1214,7 +1216,7 @@ struct nbg_engine {
     DevBuf<SynRec> rec;    // plastic network: synapse records
     DevBuf<SynStatic> wst; // static network: weight + meta
     DevBuf<float> init_w_d; // weights reset returns to, CSC order
-    DevBuf<float> v, u, gexc, ginh, iext, rule_a, trace, ev_w;
+    DevBuf<float> v, u, gexc, ginh, iext, trace, ev_w;
     DevBuf<float2> dtab;
     DevBuf<int> gen_ptr, gen_pos, gen_src;
     DevBuf<unsigned short> gen_delay;
@@ -1298,7 +1300,6 @@ struct nbg_engine {
         n.dtab = dtab.p;
         n.dtab_len = dtab_len;
         n.sdtab_len = plastic && n_rules > 0 ? std::min(dtab_len, kSharedDecayEntries) : 0;
-        n.rule_a = rule_a.p;
         n.mask = mask.p;
         n.wsum = wsum.p;
         n.Ws = Ws;
@@ -2055,6 +2056,10 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
             r.w = w[p];
             r.meta = meta;
             r.wmax = d->max_weight[s];
+            if (d->rule[s] >= 0) {
+                r.a_pre = d->rules[d->rule[s]].max_ltd;
+                r.a_post = d->rules[d->rule[s]].max_ltp;
+            }
         } else {
             wsts[(size_t)p] = SynStatic{w[p], meta};
         }
@@ -2239,14 +2244,7 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
         chk(e->ev_pos.alloc((size_t)e->ev_cap), "event log");
         chk(e->ev_w.alloc((size_t)e->ev_cap), "event log");
     }
-    {
-        std::vector<float> ra((size_t)std::max(1, e->n_rules) * 2, 0.0f);
-        for (int r = 0; r < e->n_rules; ++r) {
-            ra[r * 2 + 0] = e->rules[r].max_ltp;
-            ra[r * 2 + 1] = e->rules[r].max_ltd;
-        }
-        chk(e->rule_a.upload(ra), "rule params");
-    }
+
     if (st != NBG_OK) return bail(st);
     st = upload_layers(e);
     if (st == NBG_OK) st = ensure_decay_table(e, 4096);
