@@ -129,31 +129,6 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
                                       const float *theta, const nbg_lif_grad_params *p, int B, int N, int *err,
                                       void *stream);
 
-/* A whole checkpoint segment of the backward in one launch, B = 128 and
- * N = 512 or 1024: the L steps t = t0 + L - 1 .. t0 of
- * nbg_lif_adjoint_step_fused, each separated from the next by a grid-wide
- * barrier instead of a kernel launch, with every CTA's W tiles held in shared
- * memory for the whole segment.  Results are identical to L calls of
- * nbg_lif_adjoint_step_fused.
- *   dI_hi0/dI_lo0, dI_hi1/dI_lo1  the split dI operand of even and odd steps
- *                  (step t reads the buffer of t + 1, writes that of t)
- *   coef           the readout coefficients of every step of the run (c[t])
- *   u, m, vprev, dI  L x B x N, slice k for step t0 + k; s likewise, the
- *                  spikes s_{t0+k} (the replay's S[1..L])
- *   has_next       0 when the segment ends the run (its last step has no
- *                  recurrent term), else 1
- *   sync           two unsigned ints of device memory (the barrier counter
- *                  and its give-up flag), zeroed by this call on the stream
- * The launch is cooperative (all 8 * N / 128 CTAs resident at once).  A
- * bounded wait that gives up sets kUmmaTimeout (4) in *err; the results are
- * then invalid.  No counterpart in the reference (it has no adjoint). */
-nbg_status nbg_lif_adjoint_segment(const void *w_hi, const void *w_lo, void *dI_hi0, void *dI_lo0, void *dI_hi1,
-                                   void *dI_lo1, const float *g_read, const float *coef, const float *u,
-                                   const float *s, const uint8_t *m, const float *vprev, float *lam_v, float *dI,
-                                   float *g_theta, float *g_alpha, const float *alpha, const float *theta,
-                                   const nbg_lif_grad_params *p, int B, int N, int L, int t0, int has_next,
-                                   unsigned int *sync, int *err, void *stream);
-
 /* The recurrent weight gradient of a checkpoint segment on the tensor cores,
  * dW_rec += sum over its L steps of S_{t-1}^T dI_t, in three calls:
  *   nbg_adjoint_blocked_t   src [L][B][R] FP32 -> the R x (L*B) matrix, row r,

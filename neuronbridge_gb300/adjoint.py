@@ -61,8 +61,6 @@ _SIG = {
     "nbg_adjoint_rec_grad": (ctypes.c_int, [_vp] * 5 + [ctypes.c_int] * 3 + [_vp, _vp]),
     "nbg_lif_adjoint_step_fused": (ctypes.c_int, [_vp] * 7 + [ctypes.c_float] + [_vp] * 10 +
                                    [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp, _vp]),
-    "nbg_lif_adjoint_segment": (ctypes.c_int, [_vp] * 18 + [ctypes.POINTER(GradParams)] + [ctypes.c_int] * 5 +
-                                [_vp, _vp, _vp]),
     "nbg_adjoint_blocked_t": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
     "nbg_adjoint_wgrad": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
                                          ctypes.c_int, _vp, _vp]),
@@ -189,18 +187,6 @@ def _fused_ok(p, B: int, N: int) -> bool:
     return FUSED_STEP and _tc_ok(p, B, N) and N >= 512
 
 
-# With N = 512 or 1024 a whole checkpoint segment of the backward is one
-# cooperative launch (nbg_lif_adjoint_segment: the fused steps separated by a
-# grid barrier instead of launches), same results bit for bit.  If the device
-# refuses the launch the per-step fused launches take over.
-SEGMENT_KERNEL = True
-_SEGMENT_REFUSED = False
-
-
-def _segment_ok(p, B: int, N: int) -> bool:
-    return SEGMENT_KERNEL and not _SEGMENT_REFUSED and _fused_ok(p, B, N) and N in (512, 1024)
-
-
 def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out):
     """Forward recurrence into caller-owned buffers: the checkpoints
     ck_*[segment] (state entering each K-step segment), the readout
@@ -281,8 +267,6 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         g_parts = None if fused else torch.empty((split, B, N), device=x.device, dtype=torch.float32)
         tc_err = torch.zeros(1, device=x.device, dtype=torch.int32)
         _lib.check(lib.nbg_adjoint_rec_prepare(_ptr(w_rec), _ptr(w_hi), _ptr(w_lo), N, st))
-    seg_sync = torch.zeros(2, device=x.device, dtype=torch.int32) if fused else None
-    coef_dev = _coef_device(coef, x.device) if fused else None
     tc_w = tc and N % 256 == 0
     if tc_w:
         kk_max = L_max * B
@@ -312,16 +296,7 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                 _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
                                                     _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
                                                     ctypes.byref(p), B, N, st))
-        if fused and _segment_ok(p, B, N) and _segment(lib, w_hi, w_lo, d_hi, d_lo, g_read, coef_dev, U, S, M, VP,
-                                                      lam_v, dI, g_theta, g_alpha, alpha, theta, p, B, N, L, t0,
-                                                      have_next, seg_sync, tc_err, st):
-            have_next = True  # the whole segment ran as one launch
-            L_done = True
-        else:
-            L_done = False
         for k in reversed(range(L)):
-            if L_done:
-                break
             t = t0 + k
             if fused:  # dI_{t+1} W_rec^T and the step t that consumes it, one launch
                 cur, nxt = t & 1, (t + 1) & 1
@@ -375,26 +350,6 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
             g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
         dI_next.copy_(dI[0])
     return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), (tc_err if tc else None)
-
-
-def _segment(lib, w_hi, w_lo, d_hi, d_lo, g_read, coef_dev, U, S, M, VP, lam_v, dI, g_theta, g_alpha, alpha, theta,
-             p, B, N, L, t0, have_next, sync, err, st) -> bool:
-    """One checkpoint segment of the backward as one launch; False (and the
-    per-step launches from then on) if the device refuses the launch."""
-    global _SEGMENT_REFUSED
-    plane = B * N
-    st_code = lib.nbg_lif_adjoint_segment(
-        _ptr(w_hi), _ptr(w_lo), _ptr(d_hi[0]), _ptr(d_lo[0]), _ptr(d_hi[1]), _ptr(d_lo[1]), _ptr(g_read),
-        _ptr(coef_dev), _ptr(U), ctypes.c_void_p(S.data_ptr() + 4 * plane), _ptr(M), _ptr(VP), _ptr(lam_v), _ptr(dI),
-        _ptr(g_theta), _ptr(g_alpha), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, L, t0, int(bool(have_next)),
-        _ptr(sync), _ptr(err), st)
-    if st_code == 0:
-        return True
-    if st_code == 2:  # NBG_ERR_CUDA: the cooperative cluster launch was refused
-        _SEGMENT_REFUSED = True
-        return False
-    _lib.check(st_code)
-    return False
 
 
 def _check_tc(err) -> None:

@@ -442,247 +442,6 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     }
 }
 
-// A whole checkpoint segment of the backward in one launch: the L steps of
-// k_adj_step_umma, t = t0 + L - 1 down to t0, with a grid-wide barrier
-// between steps.  The grid, clusters and arithmetic are k_adj_step_umma's, so
-// every step's results are the same bit for bit; what changes is that each
-// CTA loads its W tiles (its 128 rows of W over its K range, hi and lo) into
-// shared memory once, and that the step boundary is a barrier instead of a
-// kernel launch.  Shared memory: the W region, and one region that holds the
-// step's dI tiles and, once the products are done, the partial accumulator
-// (the next step's copies start only after every peer has read it).
-//
-// Grid barrier: each CTA, after its threads' stores (and a proxy fence, as
-// the next step reads dI with bulk copies), adds one to sync[0] and waits
-// until it reaches (step + 1) * CTAs.  The wait is bounded: on expiry the
-// CTA sets sync[1], which ends the waits of every other CTA, and the error
-// word; the launch still runs to its end, through every cluster barrier, and
-// its results are invalid.  The launch is cooperative, so all CTAs are
-// resident at once.  N must be 512 or 1024 (at most two K chunks per CTA).
-constexpr int kSegMaxIters = 2;
-constexpr int kSegRegion = 64 * 1024;
-constexpr int kSegSmemBytes = 2 * kSegRegion + 1024 + 256;
-
-// Arrive at and wait on the grid barrier `target`; every thread calls it.
-// Returns false if the barrier gave up (timeout here or elsewhere).
-__device__ __forceinline__ bool seg_grid_sync(unsigned int *sync, unsigned int target, int *ok_smem) {
-    asm volatile("fence.proxy.async.global;" ::: "memory"); // this thread's stores, for the bulk copies
-    fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        __threadfence();
-        atomicAdd(&sync[0], 1u);
-        const long long t0 = clock64();
-        while (true) {
-            unsigned int v;
-            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(&sync[0]) : "memory");
-            if (v >= target) break;
-            if (*(volatile unsigned int *)&sync[1]) {
-                ok = 0;
-                break;
-            }
-            if (clock64() - t0 > kWaitCycles) {
-                atomicExch(&sync[1], 1u);
-                ok = 0;
-                break;
-            }
-            __nanosleep(32);
-        }
-        __threadfence();
-        asm volatile("fence.proxy.async.global;" ::: "memory");
-        *ok_smem = ok;
-    }
-    __syncthreads();
-    fence_after();
-    return *ok_smem != 0;
-}
-
-__global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 1) k_adj_segment_umma(
-    const __nv_bfloat16 *__restrict__ w_hi, const __nv_bfloat16 *__restrict__ w_lo, __nv_bfloat16 *d_hi0,
-    __nv_bfloat16 *d_lo0, __nv_bfloat16 *d_hi1, __nv_bfloat16 *d_lo1, const float *__restrict__ g_read,
-    const float *__restrict__ coef, const float *__restrict__ u, const float *__restrict__ s,
-    const unsigned char *__restrict__ m, const float *__restrict__ vprev, float *__restrict__ lam_v,
-    float *__restrict__ dI, float *__restrict__ g_theta, float *__restrict__ g_alpha,
-    const float *__restrict__ alpha, const float *__restrict__ theta, nbg_lif_grad_params p, int n, int L, int t0,
-    int has_next, unsigned int *sync, int *__restrict__ err) {
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t *wreg = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *dreg = wreg + kSegRegion;
-    float *part = reinterpret_cast<float *>(dreg);
-    uint64_t *wbar = (uint64_t *)(dreg + kSegRegion);
-    uint64_t *full = wbar + 1;
-    uint64_t *done = full + 1;
-    uint32_t *tmem_slot = (uint32_t *)(done + 1);
-    volatile int *abort = (volatile int *)(tmem_slot + 1);
-    int *ok_smem = (int *)(tmem_slot + 2);
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t rank;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
-    const int mt = blockIdx.x, ks = (int)rank;
-    const int kchunks = n / kKChunk;
-    const int iters = kchunks / kAdjCluster; // 1 or 2 (the host checks)
-    const int kc0 = ks * iters;
-    const unsigned int ctas = gridDim.x * gridDim.y;
-
-    if (threadIdx.x == 0) {
-        mbar_init(wbar, 1);
-        mbar_init(full, 1);
-        mbar_init(done, 1);
-        *abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 2) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
-                     "r"(kAdjTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    fence_before();
-    __syncthreads();
-    fence_after();
-    const uint32_t tmem = *tmem_slot;
-    if (threadIdx.x == 0) { // the CTA's W tiles, once
-        mbar_expect_tx(wbar, (uint32_t)(iters * 2 * kAdjBlockA));
-        for (int it = 0; it < iters; ++it) {
-            const size_t a_blk = (size_t)mt * kchunks + kc0 + it;
-            bulk_copy(wreg + it * 2 * kAdjBlockA, (const uint8_t *)w_hi + a_blk * kAdjBlockA, kAdjBlockA, wbar);
-            bulk_copy(wreg + it * 2 * kAdjBlockA + kAdjBlockA, (const uint8_t *)w_lo + a_blk * kAdjBlockA,
-                      kAdjBlockA, wbar);
-        }
-    }
-    const int il = threadIdx.x & 127, bsub = threadIdx.x >> 7;
-    const int i = mt * kAdjM + il;
-    const float th = theta[i], al = alpha[i];
-    constexpr int kRows = 8;
-    bool grid_ok = true;
-    bool w_ready = false; // the MMA issuer has seen the W tiles arrive
-    uint32_t phase = 0;   // completed product steps: the parity of full and done
-    for (int step = 0; step < L; ++step) {
-        const int k = L - 1 - step, t = t0 + k;
-        const bool product = has_next || step > 0;
-        const __nv_bfloat16 *din_hi = ((t + 1) & 1) ? d_hi1 : d_hi0, *din_lo = ((t + 1) & 1) ? d_lo1 : d_lo0;
-        __nv_bfloat16 *dout_hi = (t & 1) ? d_hi1 : d_hi0, *dout_lo = (t & 1) ? d_lo1 : d_lo0;
-        if (product && grid_ok) {
-            if (threadIdx.x == 0) { // dI_{t+1} tiles of this CTA's K range
-                mbar_expect_tx(full, (uint32_t)(iters * 2 * kAdjBlockB));
-                for (int it = 0; it < iters; ++it) {
-                    const int kc = kc0 + it;
-                    bulk_copy(dreg + it * 2 * kAdjBlockB, (const uint8_t *)din_hi + (size_t)kc * kAdjBlockB,
-                              kAdjBlockB, full);
-                    bulk_copy(dreg + it * 2 * kAdjBlockB + kAdjBlockB, (const uint8_t *)din_lo + (size_t)kc * kAdjBlockB,
-                              kAdjBlockB, full);
-                }
-            } else if (warp == 1 && lane == 0) { // MMA issuer
-                if (!w_ready) w_ready = mbar_wait(wbar, 0, abort);
-                const bool ready = w_ready && mbar_wait(full, phase, abort);
-                if (ready) {
-                    fence_after();
-                    for (int it = 0; it < iters; ++it) {
-                        const uint32_t a_hi = smem_addr(wreg + it * 2 * kAdjBlockA);
-                        const uint32_t a_lo = a_hi + kAdjBlockA;
-                        const uint32_t b_hi = smem_addr(dreg + it * 2 * kAdjBlockB);
-                        const uint32_t b_lo = b_hi + kAdjBlockB;
-#pragma unroll
-                        for (int q = 0; q < kKChunk / 16; ++q) {
-                            mma(tmem, make_desc(a_hi + 256 * q), make_desc(b_hi + 256 * q), kAdjIdesc, (it | q) != 0);
-                            mma(tmem, make_desc(a_lo + 256 * q), make_desc(b_hi + 256 * q), kAdjIdesc, 1u);
-                            mma(tmem, make_desc(a_hi + 256 * q), make_desc(b_lo + 256 * q), kAdjIdesc, 1u);
-                        }
-                    }
-                }
-                commit(done); // arrives even when nothing was issued
-            }
-            __syncwarp();
-        }
-        // the step's elementwise operands, while the products run
-        float op_u[kRows], op_s[kRows], op_lv[kRows], op_gr[kRows], op_gt[kRows], op_ga[kRows], op_vp[kRows];
-        unsigned char op_m[kRows];
-        const size_t plane = (size_t)kAdjN * n, base_k = (size_t)k * plane;
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) {
-            const size_t idx = (size_t)(16 * ks + bsub + 2 * r) * n + i;
-            op_u[r] = u[base_k + idx];
-            op_s[r] = s[base_k + idx];
-            op_m[r] = m[base_k + idx];
-            op_vp[r] = vprev[base_k + idx];
-            op_lv[r] = lam_v[idx];
-            op_gr[r] = g_read[idx];
-            op_gt[r] = g_theta[idx];
-            op_ga[r] = g_alpha[idx];
-        }
-        const float c_t = coef[t];
-        if (product) {
-            if (grid_ok) mbar_wait(done, phase, abort);
-            phase ^= 1u;
-            __syncthreads();
-            fence_after();
-            const int q = warp & 3, h = warp >> 2;
-            if (!*abort && grid_ok) {
-#pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    float acc[16];
-                    tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * h + 16 * c16), acc);
-#pragma unroll
-                    for (int c = 0; c < 16; ++c) part[(64 * h + 16 * c16 + c) * kAdjM + 32 * q + lane] = acc[c];
-                }
-            }
-            fence_before();
-        }
-        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-        {
-            float x[kRows][kAdjCluster];
-            if (product) {
-                const uint32_t local = smem_addr(part);
-#pragma unroll
-                for (int r = 0; r < kRows; ++r) {
-                    const uint32_t off = local + (uint32_t)(((16 * ks + bsub + 2 * r) * kAdjM + il) * 4);
-#pragma unroll
-                    for (int c = 0; c < kAdjCluster; ++c) {
-                        uint32_t ra;
-                        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(off), "r"(c));
-                        asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x[r][c]) : "r"(ra));
-                    }
-                }
-            }
-#pragma unroll
-            for (int r = 0; r < kRows; ++r) {
-                const int b = 16 * ks + bsub + 2 * r;
-                const size_t idx = (size_t)b * n + i;
-                const float uu = op_u[r], ss = op_s[r], lv = op_lv[r];
-                const float dsdu = p.smooth ? p.slope * ss * (1.0f - ss) : surrogate(uu - th, p.slope);
-                float gs = c_t * op_gr[r] - lv * (uu - p.v_reset);
-                if (product) {
-                    float ge = x[r][0];
-#pragma unroll
-                    for (int c = 1; c < kAdjCluster; ++c) ge = ge + x[r][c];
-                    gs = gs + ge;
-                }
-                const float gu = gs * dsdu + lv * (1.0f - ss);
-                const float gm = op_m[r] ? gu : 0.0f;
-                dI[base_k + idx] = gm;
-                const size_t o = blocked_index(b, i, n);
-                split_bf16(gm, dout_hi[o], dout_lo[o]);
-                lam_v[idx] = gm * (1.0f - al);
-                g_theta[idx] = op_gt[r] - gs * dsdu;
-                g_alpha[idx] = op_ga[r] + gm * (p.v_rest - op_vp[r]);
-            }
-        }
-        // peers have read this CTA's partial before the region is refilled
-        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-        if (step + 1 < L) grid_ok = seg_grid_sync(sync, (unsigned int)(step + 1) * ctas, ok_smem) && grid_ok;
-    }
-    fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0 && (*abort || !grid_ok)) atomicOr(err, kUmmaTimeout);
-    if (warp == 2) {
-        fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kAdjTmemCols)
-                     : "memory");
-    }
-}
-
 // [L][B][R] FP32 -> the R x (L*B) matrix (row r, K = l*B + b) in the blocked
 // layout, split into hi and lo (lo may be null: the values are exact in BF16).
 __global__ void k_blocked_t(const float *__restrict__ src, int L, int B, int R, __nv_bfloat16 *__restrict__ hi,
@@ -932,46 +691,6 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
                                 (__nv_bfloat16 *)dI_hi_out, (__nv_bfloat16 *)dI_lo_out, g_read, c_t, u, s, m, vprev,
                                 lam_v, dI, g_theta, g_alpha, alpha, theta, *p, N, err));
     NBG_CUDA(cudaGetLastError());
-    return NBG_OK;
-}
-
-nbg_status nbg_lif_adjoint_segment(const void *w_hi, const void *w_lo, void *dI_hi0, void *dI_lo0, void *dI_hi1,
-                                   void *dI_lo1, const float *g_read, const float *coef, const float *u,
-                                   const float *s, const uint8_t *m, const float *vprev, float *lam_v, float *dI,
-                                   float *g_theta, float *g_alpha, const float *alpha, const float *theta,
-                                   const nbg_lif_grad_params *p, int B, int N, int L, int t0, int has_next,
-                                   unsigned int *sync, int *err, void *stream) {
-    if (!w_hi || !w_lo || !dI_hi0 || !dI_lo0 || !dI_hi1 || !dI_lo1 || !g_read || !coef || !u || !s || !m || !vprev ||
-        !lam_v || !dI || !g_theta || !g_alpha || !alpha || !theta || !p || !sync || !err || B != kAdjN ||
-        (N != 512 && N != 1024) || L <= 0 || t0 < 0)
-        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_adjoint_segment: bad arguments (B must be %d, N 512 or 1024)",
-                        kAdjN);
-    static bool attr_set = false;
-    if (!attr_set) {
-        NBG_CUDA(cudaFuncSetAttribute(k_adj_segment_umma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kSegSmemBytes));
-        attr_set = true;
-    }
-    NBG_CUDA(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned int), (cudaStream_t)stream));
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(N / kAdjM, kAdjCluster);
-    cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = kSegSmemBytes;
-    cfg.stream = (cudaStream_t)stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    const cudaError_t le = cudaLaunchKernelEx(&cfg, k_adj_segment_umma, (const __nv_bfloat16 *)w_hi,
-                                              (const __nv_bfloat16 *)w_lo, (__nv_bfloat16 *)dI_hi0,
-                                              (__nv_bfloat16 *)dI_lo0, (__nv_bfloat16 *)dI_hi1,
-                                              (__nv_bfloat16 *)dI_lo1, g_read, coef, u, s, m, vprev, lam_v, dI,
-                                              g_theta, g_alpha, alpha, theta, *p, N, L, t0, has_next, sync, err);
-    if (le != cudaSuccess) { // a refused launch configuration: nothing ran, clear it for later calls
-        cudaGetLastError();
-        return nbg_fail(NBG_ERR_CUDA, "nbg_lif_adjoint_segment: launch refused: %s", cudaGetErrorString(le));
-    }
     return NBG_OK;
 }
 

@@ -135,10 +135,6 @@ struct NetDev {
     unsigned int *mask;
     unsigned int *wsum; // per slot: one bit per mask word, set while that word is non-zero
     int Ws;             // summary words per slot (ceil(Wt / 32) + 1 padding word)
-    // Quad layout (static networks whose neurons have at most four mask words):
-    // every neuron with in-synapses owns four 16-byte-aligned words, read and
-    // cleared with one 16-byte access per step; the summary ring is unused.
-    int quad;
     const int *out_ptr;
     // out lists (CSR by source): packed (mask bit << out_dbits | delay -
     // out_dmin) when that fits 32 bits, else bit and delay in two arrays
@@ -732,7 +728,7 @@ __device__ __forceinline__ void mark_out(const NetDev &n, int q, int q1, unsigne
         const unsigned int slot = (t + dl) % (unsigned int)n.D;
         const unsigned int wd = bit >> 5;
         atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit & 31u));
-        if (!n.quad) atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+        atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
     }
 }
 
@@ -915,12 +911,6 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             if (B > 2) sbC = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw);
             if (sbA) fwA = n.mask[(size_t)slot0 * n.Wt + woff + __ffs(sbA) - 1];
             if (sbB) fwB = n.mask[(size_t)wrap_slot(slot0 + 1u, D) * n.Wt + woff + __ffs(sbB) - 1];
-        } else if (n.quad) {
-            const uint4 q = *reinterpret_cast<const uint4 *>(n.mask + (size_t)slot0 * n.Wt + woff);
-            w_cur[0] = q.x;
-            w_cur[1] = q.y;
-            w_cur[2] = q.z;
-            w_cur[3] = q.w;
         } else {
             sb_cur = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
             if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
@@ -962,19 +952,6 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                     sbB = sbC;
                     fwB = fwC;
                     sbC = sbD;
-                } else if (n.quad) {
-#pragma unroll
-                    for (int k = 0; k < kWide; ++k) wc[k] = w_cur[k];
-                    sb = (wc[0] ? 1u : 0u) | (wc[1] ? 2u : 0u) | (wc[2] ? 4u : 0u) | (wc[3] ? 8u : 0u);
-                    if (sb) *reinterpret_cast<uint4 *>(mrow) = make_uint4(0u, 0u, 0u, 0u);
-                    if (b + 1 < B && nw > 0) { // the four words of step b + 1
-                        const uint4 q =
-                            *reinterpret_cast<const uint4 *>(n.mask + (size_t)wrap_slot(slot + 1u, D) * n.Wt + woff);
-                        w_cur[0] = q.x;
-                        w_cur[1] = q.y;
-                        w_cur[2] = q.z;
-                        w_cur[3] = q.w;
-                    }
                 } else {
                     sb = sb_cur;
 #pragma unroll
@@ -1005,7 +982,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                         gwords |= 1u << (n.gen_pos[g] >> 5);
                     }
                 unsigned int need = sb | gwords;
-                if (sb && !n.quad) summary_clear(n.wsum + (size_t)slot * n.Ws, woff, sb);
+                if (sb) summary_clear(n.wsum + (size_t)slot * n.Ws, woff, sb);
                 const int wfirst = __ffs(sb) - 1; // deep: the word already loaded (fw), -1 if none
                 while (need) {
                     const int wi = __ffs(need) - 1;
@@ -1022,7 +999,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                         } else {
                             word = mrow[wi];
                         }
-                        if (!n.quad) mrow[wi] = 0u; // quad: cleared with one 16-byte store above
+                        mrow[wi] = 0u;
                     }
                     for (unsigned int gf = gfired; gf; gf &= gf - 1u) {
                         const int q = __ffs(gf) - 1;
@@ -1145,7 +1122,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                 for (unsigned int m = steps[k]; m; m &= m - 1u) {
                     const unsigned int slot = wrap_slot(slot0 + (unsigned int)(__ffs(m) - 1) + dl[k], D);
                     atomicOr(&n.mask[(size_t)slot * n.Wt + wd], 1u << (bit[k] & 31u));
-                    if (!n.quad) atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
+                    atomicOr(&n.wsum[(size_t)slot * n.Ws + (wd >> 5)], 1u << (wd & 31u));
                 }
             }
         }
@@ -1245,7 +1222,6 @@ struct nbg_engine {
     DevBuf<unsigned short> gen_delay;
     DevBuf<int> last, csc_ptr_d, woff, out_ptr, out_ids, out_t, err, run_t0, trace_slot, ev_t, ev_pos;
     DevBuf<unsigned int> mask, wsum, out_bit, out_pk;
-    bool quad = false; // quad mask layout (NetDev::quad)
     int out_dbits = 0, out_dmin = 0;
     int Ws = 1;
     DevBuf<unsigned short> out_delay;
@@ -1327,7 +1303,6 @@ struct nbg_engine {
         n.mask = mask.p;
         n.wsum = wsum.p;
         n.Ws = Ws;
-        n.quad = quad ? 1 : 0;
         n.out_ptr = out_ptr.p;
         n.out_pk = out_pk.p;
         n.out_dbits = out_dbits;
@@ -2067,16 +2042,6 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     e->init_w = w;
     e->plastic = false;
     for (int64_t s = 0; s < S && !e->plastic; ++s) e->plastic = d->rule[s] >= 0;
-    {   // quad layout for static networks with at most four words per neuron
-        int nw_max = 0;
-        for (int j = 0; j < e->N; ++j) nw_max = std::max(nw_max, woff[j + 1] - woff[j]);
-        e->quad = !e->plastic && nw_max <= 4;
-        if (e->quad) {
-            for (int j = 0; j < e->N; ++j) woff[j + 1] = woff[j] + (cptr[j + 1] > cptr[j] ? 4 : 0);
-            e->Wt = std::max(woff[e->N], 4);
-            e->woff_host = woff;
-        }
-    }
     // synapse records: 32 bytes with the STDP state when anything learns
     std::vector<SynRec> recs;
     std::vector<SynStatic> wsts;

@@ -314,30 +314,3 @@ def test_fused_adjoint_step_equals_two_launch_form(monkeypatch):
     for name, g, r in zip(("w_in", "w_rec", "w_out", "alpha", "theta"), fused, ref_params):
         scale = r.grad.abs().max().item()
         assert (g.double().cpu() - r.grad).abs().max().item() <= 1e-3 * scale, name
-
-
-@pytest.mark.gpu
-@pytest.mark.parametrize("n_rec", [512, 1024])
-def test_segment_backward_equals_per_step_launches(monkeypatch, n_rec):
-    """B = 128, N = 512 and 1024, spiking mode: each checkpoint segment of the
-    backward as one cooperative launch (nbg_lif_adjoint_segment, grid barrier
-    between steps) gives the same gradients, bit for bit, as one fused launch
-    per step; T = 60 with checkpoints every 20 covers the segment that ends
-    the run (no recurrent term in its last step) and the segments before it."""
-    from neuronbridge_gb300 import adjoint
-    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
-
-    kw = dict(n_in=64, n_rec=n_rec, n_out=5, checkpoint=20, seed=11)
-    torch.manual_seed(0)
-    model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, **kw, **SPIKING)
-    rates = torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0
-    x = poisson_inputs(rates, T, 128, dt=1.0, seed=3)
-    labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
-    assert adjoint._segment_ok(model.params, 128, n_rec)
-    loss_s, seg = _grads(model, x, labels)
-    assert not adjoint._SEGMENT_REFUSED, "the device refused the cooperative segment launch"
-    monkeypatch.setattr(adjoint, "SEGMENT_KERNEL", False)
-    loss_f, fused = _grads(model, x, labels)
-    assert loss_s == loss_f
-    for g, h in zip(seg, fused):
-        assert torch.equal(g, h)
