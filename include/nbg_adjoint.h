@@ -131,24 +131,39 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
 
 /* The recurrent weight gradient of a checkpoint segment on the tensor cores,
  * dW_rec += sum over its L steps of S_{t-1}^T dI_t, in three calls:
- *   nbg_adjoint_blocked_t   src [L][B][R] FP32 -> the R x (L*B) matrix, row r,
- *                           column l*B + b, blocked BF16; split into hi and lo
- *                           when lo is not NULL (else the values must be
- *                           exact in BF16, as spikes are).  R a multiple of
- *                           128, L*B of 64.
+ *   nbg_adjoint_blocked_t   src [L][B][R] FP32 -> the R_pad x (L*B) matrix,
+ *                           row r, column l*B + b, blocked BF16, rows R ..
+ *                           R_pad - 1 zero; split into hi and lo when lo is
+ *                           not NULL (else the values must be exact in BF16,
+ *                           as spikes are).  R_pad >= R a multiple of 128,
+ *                           L*B a multiple of 64.
  *   nbg_adjoint_wgrad       part[split][Nc][M] = split-K partials of
  *                           (a_hi + a_lo)(b + b_lo)^T without the lo x lo
  *                           term (b_lo NULL: b exact), a: M x K, b: Nc x K (from
  *                           nbg_adjoint_blocked_t), M a multiple of 128, Nc
  *                           of 256, K of 64; *err gets 4 if a bounded wait
  *                           gave up
- *   nbg_adjoint_reduce_add  g[e] += sum over q, in order, of part[q][e]
+ *   nbg_adjoint_reduce_add  g[e] += sum over q, in order, of part[q * stride
+ *                           + e], e < count (stride >= count: the partials of
+ *                           a padded Nc keep their padding rows after the
+ *                           gradient's)
  * With a = dI^T (split) and b = S^T (or X^T, split) part[q] is laid out as
- * dW_rec (or dW_in): row = presynaptic neuron (or input channel). */
-nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, void *hi, void *lo, void *stream);
+ * dW_rec (or dW_in): row = presynaptic neuron (or input channel).  A row
+ * count that is not a multiple of the tile (Nc of 256) is padded with zero
+ * rows by nbg_adjoint_blocked_t; the padding rows of part are not added. */
+nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, int R_pad, void *hi, void *lo,
+                                 void *stream);
 nbg_status nbg_adjoint_wgrad(const void *a_hi, const void *a_lo, const void *b, const void *b_lo, int M, int Nc,
                              int K, float *part, int split, int *err, void *stream);
-nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_t count, void *stream);
+nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_t count, int64_t stride,
+                                  void *stream);
+
+/* C = A B for the readout's small products (B x N by N x O, its transposes):
+ * element (r, c) of A at A[r * a_rs + c * a_cs], likewise B; C is M x N row
+ * major.  One thread per output, the sum over k in ascending order in FP32, so
+ * results do not depend on the launch.  No counterpart in the reference. */
+nbg_status nbg_small_gemm(const float *A, int a_rs, int a_cs, const float *B, int b_rs, int b_cs, float *C, int M,
+                          int N, int K, void *stream);
 
 /* Poisson input spikes x[t][b][c] in {0, 1}: channel c fires with
  * probability min(1, rate_c * dt * 1e-3) from the PoissonRate hash of

@@ -61,10 +61,13 @@ _SIG = {
     "nbg_adjoint_rec_grad": (ctypes.c_int, [_vp] * 5 + [ctypes.c_int] * 3 + [_vp, _vp]),
     "nbg_lif_adjoint_step_fused": (ctypes.c_int, [_vp] * 7 + [ctypes.c_float] + [_vp] * 10 +
                                    [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp, _vp]),
-    "nbg_adjoint_blocked_t": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "nbg_adjoint_blocked_t": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp,
+                                             _vp]),
+    "nbg_small_gemm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_adjoint_wgrad": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp,
                                          ctypes.c_int, _vp, _vp]),
-    "nbg_adjoint_reduce_add": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int64, _vp]),
+    "nbg_adjoint_reduce_add": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _vp]),
 }
 _LIB = None
 
@@ -224,7 +227,15 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
             _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
                                                 float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
             s_prev = s
-    torch.mm(z, w_out, out=out)
+    _readout(lib, z, w_out, out, st)
+
+
+def _readout(lib, z, w_out, out, st) -> None:
+    """out = z W_out (B x N by N x O) with the engine's small deterministic
+    product."""
+    B, N = z.shape
+    O = w_out.shape[1]
+    _lib.check(lib.nbg_small_gemm(_ptr(z), N, 1, _ptr(w_out), O, 1, _ptr(out), B, O, N, st))
 
 
 def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref, ck_s, p, K, coef):
@@ -235,8 +246,11 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     T, B, C = x.shape
     N = w_rec.shape[0]
     st = _stream()
-    g_read = gy @ w_out.t()
-    g_w_out = z.t() @ gy
+    O = w_out.shape[1]
+    g_read = torch.empty((B, N), device=x.device, dtype=torch.float32)  # gy W_out^T
+    g_w_out = torch.empty((N, O), device=x.device, dtype=torch.float32)  # z^T gy
+    _lib.check(lib.nbg_small_gemm(_ptr(gy), O, 1, _ptr(w_out), 1, O, _ptr(g_read), B, N, O, st))
+    _lib.check(lib.nbg_small_gemm(_ptr(z), 1, N, _ptr(gy), O, 1, _ptr(g_w_out), N, O, B, st))
     g_w_in = torch.zeros_like(w_in)
     g_w_rec = torch.zeros_like(w_rec)
     lam_v = torch.zeros((B, N), device=x.device, dtype=torch.float32)
@@ -267,18 +281,19 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         g_parts = None if fused else torch.empty((split, B, N), device=x.device, dtype=torch.float32)
         tc_err = torch.zeros(1, device=x.device, dtype=torch.int32)
         _lib.check(lib.nbg_adjoint_rec_prepare(_ptr(w_rec), _ptr(w_hi), _ptr(w_lo), N, st))
-    tc_w = tc and N % 256 == 0
+    # weight gradients on the tensor cores: the product's column operand (S^T,
+    # X^T) is padded with zero rows to a multiple of 256
+    tc_w = tc_in = tc
     if tc_w:
         kk_max = L_max * B
+        N256, C256 = -(-N // 256) * 256, -(-C // 256) * 256
         dT_hi = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
         dT_lo = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
-        sT = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
-        tc_in = C % 256 == 0
-        w_part = torch.empty(max(WGRAD_SPLIT * N * N, WGRAD_IN_SPLIT * C * N if tc_in else 0), device=x.device,
+        sT = torch.empty(N256 * kk_max, device=x.device, dtype=torch.bfloat16)
+        w_part = torch.empty(max(WGRAD_SPLIT * N256 * N, WGRAD_IN_SPLIT * C256 * N), device=x.device,
                              dtype=torch.float32)
-        if tc_in:
-            xT_hi = torch.empty(C * kk_max, device=x.device, dtype=torch.bfloat16)
-            xT_lo = torch.empty(C * kk_max, device=x.device, dtype=torch.bfloat16)
+        xT_hi = torch.empty(C256 * kk_max, device=x.device, dtype=torch.bfloat16)
+        xT_lo = torch.empty(C256 * kk_max, device=x.device, dtype=torch.bfloat16)
     segments = list(enumerate(range(0, T, K)))
     for seg, t0 in reversed(segments):
         t1 = min(T, t0 + K)
@@ -332,20 +347,20 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                                                 _ptr(theta), ctypes.byref(p), B, N, st))
             have_next = True
         if tc_w:
-            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, _ptr(dT_hi), _ptr(dT_lo), st))
-            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(S), L, B, N, _ptr(sT), None, st))
+            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, N, _ptr(dT_hi), _ptr(dT_lo), st))
+            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(S), L, B, N, N256, _ptr(sT), None, st))
             ws = min(WGRAD_SPLIT, L * B // 64)
-            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(sT), None, N, N, L * B, _ptr(w_part), ws,
-                                             _ptr(tc_err), st))
-            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_rec), _ptr(w_part), ws, N * N, st))
+            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(sT), None, N, N256, L * B, _ptr(w_part),
+                                             ws, _ptr(tc_err), st))
+            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_rec), _ptr(w_part), ws, N * N, N256 * N, st))
         else:
             g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
         if tc_w and tc_in:
             ws = min(WGRAD_IN_SPLIT, L * B // 64)
-            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x[t0:t1]), L, B, C, _ptr(xT_hi), _ptr(xT_lo), st))
-            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(xT_hi), _ptr(xT_lo), N, C, L * B,
+            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x[t0:t1]), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), st))
+            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(xT_hi), _ptr(xT_lo), N, C256, L * B,
                                              _ptr(w_part), ws, _ptr(tc_err), st))
-            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_in), _ptr(w_part), ws, C * N, st))
+            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_in), _ptr(w_part), ws, C * N, C256 * N, st))
         else:
             g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
         dI_next.copy_(dI[0])

@@ -376,7 +376,31 @@ __global__ void k_poisson(float *__restrict__ x, const float *__restrict__ rates
 
 } // namespace
 
+// C[i][j] = sum over k, ascending, of A[i][k] B[k][j] (element (r, c) of A at
+// A[r * a_rs + c * a_cs], likewise B): one thread per output, sequential FP32
+// sums, so the result does not depend on the launch.  For the readout's small
+// products (B x N by N x O and the like).
+__global__ void k_small_gemm(const float *__restrict__ A, int a_rs, int a_cs, const float *__restrict__ Bm, int b_rs,
+                             int b_cs, float *__restrict__ Cm, int M, int N, int K) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= (long long)M * N) return;
+    const int i = (int)(o / N), j = (int)(o % N);
+    float acc = 0.0f;
+    for (int k = 0; k < K; ++k) acc = acc + A[(size_t)i * a_rs + (size_t)k * a_cs] * Bm[(size_t)k * b_rs + (size_t)j * b_cs];
+    Cm[o] = acc;
+}
+
 extern "C" {
+
+nbg_status nbg_small_gemm(const float *A, int a_rs, int a_cs, const float *B, int b_rs, int b_cs, float *C, int M,
+                          int N, int K, void *stream) {
+    if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0) return nbg_fail(NBG_ERR_INVALID, "nbg_small_gemm: bad arguments");
+    const long long total = (long long)M * N;
+    k_small_gemm<<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)stream>>>(A, a_rs, a_cs, B, b_rs, b_cs, C, M,
+                                                                                   N, K);
+    NBG_CUDA(cudaGetLastError());
+    return NBG_OK;
+}
 
 nbg_status nbg_lif_forward_step(const float *I, float *v, int32_t *ref, float *s_out, float *u_rec, uint8_t *m_rec,
                                 float *vprev_rec, float *z, float c_t, const float *alpha, const float *theta,

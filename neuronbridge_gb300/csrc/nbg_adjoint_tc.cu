@@ -444,16 +444,18 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
 
 // [L][B][R] FP32 -> the R x (L*B) matrix (row r, K = l*B + b) in the blocked
 // layout, split into hi and lo (lo may be null: the values are exact in BF16).
-__global__ void k_blocked_t(const float *__restrict__ src, int L, int B, int R, __nv_bfloat16 *__restrict__ hi,
-                            __nv_bfloat16 *__restrict__ lo) {
+// Rows R .. R_pad - 1 of the result are zero (padding to the product's tile).
+__global__ void k_blocked_t(const float *__restrict__ src, int L, int B, int R, int R_pad,
+                            __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)L * B * R;
+    const long long total = (long long)L * B * R_pad;
     if (idx >= total) return;
-    const int r = (int)(idx % R);
-    const int kk = (int)(idx / R); // l * B + b
+    const int r = (int)(idx % R_pad);
+    const int kk = (int)(idx / R_pad); // l * B + b
     const size_t o = blocked_index(r, kk, L * B);
-    if (lo) split_bf16(src[idx], hi[o], lo[o]);
-    else hi[o] = __float2bfloat16_rn(src[idx]);
+    const float v = r < R ? src[(size_t)kk * R + r] : 0.0f;
+    if (lo) split_bf16(v, hi[o], lo[o]);
+    else hi[o] = __float2bfloat16_rn(v);
 }
 
 constexpr int kWgN = 256; // UMMA N of the weight-gradient product
@@ -582,11 +584,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-__global__ void k_reduce_add(float *__restrict__ g, const float *__restrict__ part, int split, long long count) {
+__global__ void k_reduce_add(float *__restrict__ g, const float *__restrict__ part, int split, long long count,
+                             long long stride) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count) return;
     float acc = part[idx];
-    for (int q = 1; q < split; ++q) acc = acc + part[(size_t)q * count + idx];
+    for (int q = 1; q < split; ++q) acc = acc + part[(size_t)q * stride + idx];
     g[idx] = g[idx] + acc;
 }
 
@@ -694,13 +697,14 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
     return NBG_OK;
 }
 
-nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, void *hi, void *lo, void *stream) {
-    if (!src || !hi || L <= 0 || B <= 0 || R <= 0 || R % kAdjM || ((long long)L * B) % kKChunk)
-        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_blocked_t: R must be a multiple of %d and L*B of %d", kAdjM,
-                        kKChunk);
-    const long long total = (long long)L * B * R;
+nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, int R_pad, void *hi, void *lo,
+                                 void *stream) {
+    if (!src || !hi || L <= 0 || B <= 0 || R <= 0 || R_pad < R || R_pad % kAdjM || ((long long)L * B) % kKChunk)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_blocked_t: R_pad must be >= R and a multiple of %d, L*B a "
+                        "multiple of %d", kAdjM, kKChunk);
+    const long long total = (long long)L * B * R_pad;
     k_blocked_t<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        src, L, B, R, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo);
+        src, L, B, R, R_pad, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }
@@ -735,9 +739,12 @@ nbg_status nbg_adjoint_wgrad(const void *a_hi, const void *a_lo, const void *b, 
     return NBG_OK;
 }
 
-nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_t count, void *stream) {
-    if (!g || !part || split <= 0 || count <= 0) return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_reduce_add: bad arguments");
-    k_reduce_add<<<(unsigned)((count + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g, part, split, (long long)count);
+nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_t count, int64_t stride,
+                                  void *stream) {
+    if (!g || !part || split <= 0 || count <= 0 || stride < count)
+        return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_reduce_add: bad arguments");
+    k_reduce_add<<<(unsigned)((count + 255) / 256), 256, 0, (cudaStream_t)stream>>>(g, part, split, (long long)count,
+                                                                                 (long long)stride);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

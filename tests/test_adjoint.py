@@ -314,3 +314,32 @@ def test_fused_adjoint_step_equals_two_launch_form(monkeypatch):
     for name, g, r in zip(("w_in", "w_rec", "w_out", "alpha", "theta"), fused, ref_params):
         scale = r.grad.abs().max().item()
         assert (g.double().cpu() - r.grad).abs().max().item() <= 1e-3 * scale, name
+
+
+@pytest.mark.gpu
+def test_tensor_core_weight_gradients_padded_shapes(monkeypatch):
+    """N = 384 and C = 100 (not multiples of the weight-gradient tile of 256):
+    the tensor-core weight gradients pad S^T and X^T with zero rows, and the
+    gradients stay within the FP64 tolerance and agree with the cuBLAS FP32
+    path."""
+    from neuronbridge_gb300 import adjoint
+    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+
+    kw = dict(n_in=100, n_rec=384, n_out=5, checkpoint=20, seed=11)
+    torch.manual_seed(0)
+    model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, **kw, **SPIKING)
+    rates = torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0
+    x = poisson_inputs(rates, T, 128, dt=1.0, seed=3)
+    labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
+    assert adjoint._tc_ok(model.params, 128, 384)
+    loss_tc, tc = _grads(model, x, labels)
+    monkeypatch.setattr(adjoint, "_tc_ok", lambda p, B, N: False)
+    loss_fp32, fp32 = _grads(model, x, labels)
+    assert loss_tc == loss_fp32
+    ref_params = [p.detach().double().cpu().requires_grad_(True) for p in _params(model)]
+    ref_loss = _ref_loss(model, x.double().cpu(), labels.cpu(), ref_params, False)
+    ref_loss.backward()
+    for name, g, h, r in zip(("w_in", "w_rec", "w_out", "alpha", "theta"), tc, fp32, ref_params):
+        scale = r.grad.abs().max().item()
+        assert (g.double().cpu() - r.grad).abs().max().item() <= 1e-3 * scale, name
+        assert (g - h).abs().max().item() <= 1e-3 * h.abs().max().item(), name
