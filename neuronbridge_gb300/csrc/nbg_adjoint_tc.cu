@@ -444,18 +444,41 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
 
 // [L][B][R] FP32 -> the R x (L*B) matrix (row r, K = l*B + b) in the blocked
 // layout, split into hi and lo (lo may be null: the values are exact in BF16).
-// Rows R .. R_pad - 1 of the result are zero (padding to the product's tile).
-__global__ void k_blocked_t(const float *__restrict__ src, int L, int B, int R, int R_pad,
-                            __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)L * B * R_pad;
-    if (idx >= total) return;
-    const int r = (int)(idx % R_pad);
-    const int kk = (int)(idx / R_pad); // l * B + b
-    const size_t o = blocked_index(r, kk, L * B);
-    const float v = r < R ? src[(size_t)kk * R + r] : 0.0f;
-    if (lo) split_bf16(v, hi[o], lo[o]);
-    else hi[o] = __float2bfloat16_rn(v);
+// [L][B][R] FP32 -> the R_pad x (L*B) matrix (row r, K = l*B + b) in the
+// blocked layout, split into hi and lo (lo may be null: the values are exact
+// in BF16); rows R .. R_pad - 1 are zero (padding to the product's tile).
+// One CTA per 128-row x 64-K output block: the 64 x 128 source tile is read
+// with coalesced loads into shared memory, and the block -- 16 KiB,
+// contiguous in the blocked layout -- is written one 16-byte core-matrix row
+// (8 K values of one row) per store.
+constexpr int kBtThreads = 256;
+__global__ void __launch_bounds__(kBtThreads) k_blocked_t(const float *__restrict__ src, int L, int B, int R,
+                                                          int R_pad, __nv_bfloat16 *__restrict__ hi,
+                                                          __nv_bfloat16 *__restrict__ lo) {
+    __shared__ float tile[kKChunk][kAdjM + 1];
+    const int rb = blockIdx.x, kb = blockIdx.y, KK = L * B;
+    for (int e = threadIdx.x; e < kKChunk * kAdjM; e += kBtThreads) {
+        const int kk = e / kAdjM, rr = e % kAdjM; // r fastest: coalesced along the source row
+        const int r = rb * kAdjM + rr;
+        tile[kk][rr] = r < R ? src[(size_t)(kb * kKChunk + kk) * R + r] : 0.0f;
+    }
+    __syncthreads();
+    const size_t blk = ((size_t)rb * (size_t)(KK / kKChunk) + (size_t)kb) * (size_t)(kAdjM * kKChunk);
+    // 1,024 core-matrix rows of 8 values; element e of the block:
+    //   k & 7 = e & 7, row & 7 = (e >> 3) & 7, k >> 3 = (e >> 6) & 7, row >> 3 = e >> 9
+    for (int c = threadIdx.x; c < kAdjM * kKChunk / 8; c += kBtThreads) {
+        const int e0 = c * 8;
+        const int row = ((e0 >> 9) << 3) | ((e0 >> 3) & 7), k0 = ((e0 >> 6) & 7) << 3;
+        __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float v = tile[k0 + q][row];
+            if (lo) split_bf16(v, h[q], l[q]);
+            else h[q] = __float2bfloat16_rn(v);
+        }
+        reinterpret_cast<uint4 *>(hi + blk)[c] = *reinterpret_cast<const uint4 *>(h);
+        if (lo) reinterpret_cast<uint4 *>(lo + blk)[c] = *reinterpret_cast<const uint4 *>(l);
+    }
 }
 
 constexpr int kWgN = 256; // UMMA N of the weight-gradient product
@@ -702,9 +725,9 @@ nbg_status nbg_adjoint_blocked_t(const float *src, int L, int B, int R, int R_pa
     if (!src || !hi || L <= 0 || B <= 0 || R <= 0 || R_pad < R || R_pad % kAdjM || ((long long)L * B) % kKChunk)
         return nbg_fail(NBG_ERR_INVALID, "nbg_adjoint_blocked_t: R_pad must be >= R and a multiple of %d, L*B a "
                         "multiple of %d", kAdjM, kKChunk);
-    const long long total = (long long)L * B * R_pad;
-    k_blocked_t<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-        src, L, B, R, R_pad, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo);
+    const dim3 grid(R_pad / kAdjM, (unsigned)(((long long)L * B) / kKChunk));
+    k_blocked_t<<<grid, kBtThreads, 0, (cudaStream_t)stream>>>(src, L, B, R, R_pad, (__nv_bfloat16 *)hi,
+                                                               (__nv_bfloat16 *)lo);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }
