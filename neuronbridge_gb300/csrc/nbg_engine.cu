@@ -294,22 +294,27 @@ struct Syn {
     unsigned int meta;
 };
 
+// A plastic synapse record from its two 16-byte halves.
+__device__ __forceinline__ Syn syn_decode(const uint4 a, const uint4 b) {
+    Syn y;
+    y.w = __uint_as_float(a.x);
+    y.apre = __uint_as_float(a.y);
+    y.apost = __uint_as_float(a.z);
+    y.last = (int)a.w;
+    y.meta = b.x;
+    y.wmax = __uint_as_float(b.y);
+    y.a_pre = __uint_as_float(b.z);
+    y.a_post = __uint_as_float(b.w);
+    return y;
+}
+
 // Load synapse s: the whole 32-byte record of a plastic network (two 16-byte
 // loads of one sector, issued together), or the 8-byte static record.
 template <class S>
 __device__ __forceinline__ Syn load_syn(const NetDev &n, int s) {
     Syn y;
     if (S::plastic(n)) {
-        const uint4 a = reinterpret_cast<const uint4 *>(n.rec + s)[0];
-        const uint4 b = reinterpret_cast<const uint4 *>(n.rec + s)[1];
-        y.w = __uint_as_float(a.x);
-        y.apre = __uint_as_float(a.y);
-        y.apost = __uint_as_float(a.z);
-        y.last = (int)a.w;
-        y.meta = b.x;
-        y.wmax = __uint_as_float(b.y);
-        y.a_pre = __uint_as_float(b.z);
-        y.a_post = __uint_as_float(b.w);
+        y = syn_decode(reinterpret_cast<const uint4 *>(n.rec + s)[0], reinterpret_cast<const uint4 *>(n.rec + s)[1]);
     } else {
         const uint2 a = reinterpret_cast<const uint2 *>(n.wst)[s];
         y.w = __uint_as_float(a.x);
@@ -514,6 +519,23 @@ __device__ __forceinline__ void apply_word(const NetDev &n, const Model &M, Neur
     for (; word; word &= word - 1u) apply_arrival<S>(n, M, r, acc_a, acc_b, gate, first + __ffs(word) - 1, t);
 }
 
+// apply_word for the deep drain: the record of synapse pos_cur was copied
+// into shared memory (srec) a step ahead; an arrival on pos_nxt, the synapse
+// whose copy for the next step is in flight, makes that copy stale.
+template <class S>
+__device__ __forceinline__ void apply_word_staged(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
+                                                  float &acc_b, bool gate, unsigned int word, int first, int t,
+                                                  int pos_cur, const uint4 *srec, int &pos_nxt) {
+    for (; word; word &= word - 1u) {
+        const int s = first + __ffs(word) - 1;
+        Syn y;
+        if (s == pos_cur) y = syn_decode(srec[0], srec[1]);
+        else y = load_syn<S>(n, s);
+        if (s == pos_nxt) pos_nxt = -1;
+        apply_loaded<S>(n, M, r, acc_a, acc_b, gate, s, y, t);
+    }
+}
+
 // One neuron update; returns true on a spike.  `noise` is
 // sigma * gauss12(noise_key(seed, j), t) for noisy IZH_RK4 layers (else 0).
 template <class S>
@@ -684,6 +706,39 @@ __device__ __forceinline__ unsigned int summary_bits(const unsigned int *srow, i
     if (sh + nw > 32) x |= (unsigned long long)srow[w0 + 1] << 32;
     x >>= sh;
     return nw >= 32 ? (unsigned int)x : (unsigned int)x & ((1u << nw) - 1u);
+}
+
+// The same bits from the one or two summary words already read (lo = word
+// woff / 32 of the row, hi = the next word, used when the range crosses it).
+__device__ __forceinline__ unsigned int summary_decode(unsigned int lo, unsigned int hi, int woff, int nw) {
+    const unsigned long long x = ((unsigned long long)hi << 32 | lo) >> (woff & 31);
+    return nw >= 32 ? (unsigned int)x : (unsigned int)x & ((1u << nw) - 1u);
+}
+
+// Asynchronous 4-byte copy global -> shared (zero-filled when !valid, which
+// reads nothing): the drain's look-ahead words land in shared memory instead
+// of registers, so no instruction waits on them until they are read a step
+// later.
+__device__ __forceinline__ void stage_u32(unsigned int *dst, const unsigned int *src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((unsigned int)__cvta_generic_to_shared(dst)),
+                 "l"(__cvta_generic_to_global(src)), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void stage_16(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"((unsigned int)__cvta_generic_to_shared(dst)),
+                 "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Stage the summary words of [woff, woff+nw) in row srow.
+__device__ __forceinline__ void stage_summary(unsigned int *lo, unsigned int *hi, const unsigned int *srow, int woff,
+                                              int nw, bool valid) {
+    const int w0 = woff >> 5;
+    const bool two = valid && (woff & 31) + nw > 32;
+    stage_u32(lo, srow + w0, valid);
+    stage_u32(hi, srow + w0 + (two ? 1 : 0), two); // an address inside the row even when nothing is read
 }
 
 // Clear `bits` (relative to woff) in a summary row; neighbours share words.
@@ -890,9 +945,14 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     //   and the synapse records of the first arrivals of step b + 1 (whose
     //   word arrived during step b - 1) are prefetched into L1, so that step
     //   b + 1 finds them on the SM.  Further flagged words of a step (rare at a
-    //   few arrivals per hundred steps) are loaded when it runs.
-    // * Wide drain: the summary of step b + 2 and the first kWide flagged
-    //   words of step b + 1 are requested while step b runs, the records of
+    //   few arrivals per hundred steps) are loaded when it runs.  The
+    //   requested words travel by asynchronous copy into shared memory and
+    //   are read at the top of the next step: a load into a register would
+    //   stall the step at its first use (the summary's shift, the move that
+    //   rotates the pipeline), one memory round trip per step.
+    // * Wide drain: the summary of step b + 3 (through shared memory, as
+    //   above) and the first kWide flagged words of step b + 1 are requested
+    //   while step b runs, the records of
     //   step b + 1's arrivals are prefetched into L1 at the end of step b,
     //   and the arrivals of a word are applied kBatch per memory round trip.
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
@@ -904,13 +964,29 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     // wide: summary bits of steps b, b+1 and the first kWide words of step b (loads in flight)
     unsigned int sb_cur = 0u, sb_nxt = 0u;
     unsigned int w_cur[kWide] = {0u, 0u, 0u, 0u};
-    if (active && fast && nw > 0) {
+    // Look-ahead words in flight: [parity of the step that requested them]
+    // [summary word lo, summary word hi, first flagged mask word][thread].
+    // Each step waits for the words the step before requested, reads them
+    // and requests the next ones into the other half.
+    __shared__ unsigned int s_stage[2][3][256];
+    unsigned int *const st_lo = &s_stage[0][0][threadIdx.x];
+    constexpr int kStageHalf = 3 * 256, kStageHi = 256, kStageFw = 512;
+    // deep: the record of the next step's first arrival, [parity][thread][two
+    // 16-byte halves]; pos_nxt is its CSC position (-1: none, or stale)
+    __shared__ uint4 s_rec[S::deep ? 2 * 256 * 2 : 1];
+    int pos_nxt = -1;
+    const bool staged = active && fast && nw > 0;
+    if (staged) {
         if constexpr (S::deep) {
             sbA = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
             if (B > 1) sbB = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
-            if (B > 2) sbC = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw);
             if (sbA) fwA = n.mask[(size_t)slot0 * n.Wt + woff + __ffs(sbA) - 1];
-            if (sbB) fwB = n.mask[(size_t)wrap_slot(slot0 + 1u, D) * n.Wt + woff + __ffs(sbB) - 1];
+            // for step 0: the summary of step 2 and the first word of step 1
+            unsigned int *const h = st_lo + kStageHalf;
+            stage_summary(h, h + kStageHi, n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw, B > 2);
+            stage_u32(h + kStageFw, n.mask + (size_t)wrap_slot(slot0 + 1u, D) * n.Wt + woff + (sbB ? __ffs(sbB) - 1 : 0),
+                      sbB != 0u);
+            stage_commit();
         } else {
             sb_cur = summary_bits(n.wsum + (size_t)slot0 * n.Ws, woff, nw);
             if (B > 1) sb_nxt = summary_bits(n.wsum + (size_t)wrap_slot(slot0 + 1u, D) * n.Ws, woff, nw);
@@ -918,6 +994,9 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
 #pragma unroll
             for (int k = 0; k < kWide; ++k)
                 if ((sb_cur >> k) & 1u) w_cur[k] = r0[k];
+            unsigned int *const h = st_lo + kStageHalf; // for step 0: the summary of step 2
+            stage_summary(h, h + kStageHi, n.wsum + (size_t)wrap_slot(slot0 + 2u, D) * n.Ws, woff, nw, B > 2);
+            stage_commit();
         }
     }
     unsigned long long delivered = 0;
@@ -925,6 +1004,8 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     for (int b = 0; b < B; ++b) {
         const int t = T0 + b;
         bool spk = false;
+        const int pos_cur = pos_nxt; // deep: the staged record of this step, if any
+        pos_nxt = -1;
         if (active) {
             const unsigned int slot = wrap_slot(slot0 + (unsigned int)b, D);
             unsigned int *mrow = n.mask + (size_t)slot * n.Wt + woff;
@@ -936,34 +1017,57 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                 if constexpr (S::deep) {
                     sb = sbA;
                     fw = fwA;
-                    unsigned int fwC = 0u, sbD = 0u;
-                    if (b + 2 < B && sbC)
-                        fwC = n.mask[(size_t)wrap_slot(slot + 2u, D) * n.Wt + woff + __ffs(sbC) - 1];
-                    if (b + 3 < B && nw > 0)
-                        sbD = summary_bits(n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff, nw);
-                    if (fwB) { // the records of step b + 1's first two arrivals into L1
-                        const int p0 = base + (__ffs(sbB) - 1) * 32;
+                    if (staged) {
+                        // the words step b - 1 requested: the summary of step
+                        // b + 2 and the first flagged word of step b + 1
+                        stage_wait();
+                        const unsigned int *const h = st_lo + ((b + 1) & 1) * kStageHalf;
+                        sbC = summary_decode(h[0], h[kStageHi], woff, nw);
+                        fwB = h[kStageFw];
+                        if (b + 1 < B) { // request the summary of step b + 3 and the first word of step b + 2
+                            unsigned int *const q = st_lo + (b & 1) * kStageHalf;
+                            stage_summary(q, q + kStageHi, n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff,
+                                          nw, b + 3 < B);
+                            stage_u32(q + kStageFw,
+                                      n.mask + (size_t)wrap_slot(slot + 2u, D) * n.Wt + woff +
+                                          (sbC ? __ffs(sbC) - 1 : 0),
+                                      b + 2 < B && sbC != 0u);
+                            if (fwB) { // the record of step b + 1's first arrival
+                                pos_nxt = base + (__ffs(sbB) - 1) * 32 + __ffs(fwB) - 1;
+                                uint4 *const d = s_rec + ((b & 1) * 256 + threadIdx.x) * 2;
+                                stage_16(d, n.rec + pos_nxt);
+                                stage_16(d + 1, reinterpret_cast<const uint4 *>(n.rec + pos_nxt) + 1);
+                            }
+                            stage_commit();
+                        }
+                    }
+                    if (fwB) { // the record of its second arrival into L2
                         const unsigned int rest = fwB & (fwB - 1u);
-                        prefetch_syn<S>(n, p0 + __ffs(fwB) - 1);
-                        if (rest) prefetch_syn<S>(n, p0 + __ffs(rest) - 1);
+                        if (rest) prefetch_syn<S>(n, base + (__ffs(sbB) - 1) * 32 + __ffs(rest) - 1);
                     }
                     sbA = sbB;
                     fwA = fwB;
                     sbB = sbC;
-                    fwB = fwC;
-                    sbC = sbD;
                 } else {
                     sb = sb_cur;
 #pragma unroll
                     for (int k = 0; k < kWide; ++k) wc[k] = w_cur[k];
-                    if (b + 1 < B) { // words of step b + 1, summary of step b + 2
+                    if (b + 1 < B) { // words of step b + 1
                         const unsigned int *rn = n.mask + (size_t)wrap_slot(slot + 1u, D) * n.Wt + woff;
 #pragma unroll
                         for (int k = 0; k < kWide; ++k) w_cur[k] = ((sb_nxt >> k) & 1u) ? rn[k] : 0u;
                         sb_cur = sb_nxt;
-                        sb_nxt = (b + 2 < B && nw > 0)
-                                     ? summary_bits(n.wsum + (size_t)wrap_slot(slot + 2u, D) * n.Ws, woff, nw)
-                                     : 0u;
+                    }
+                    if (staged) { // the summary of step b + 2 (requested by step b - 1); request b + 3's
+                        stage_wait();
+                        const unsigned int *const h = st_lo + ((b + 1) & 1) * kStageHalf;
+                        sb_nxt = summary_decode(h[0], h[kStageHi], woff, nw);
+                        if (b + 1 < B) {
+                            unsigned int *const q = st_lo + (b & 1) * kStageHalf;
+                            stage_summary(q, q + kStageHi, n.wsum + (size_t)wrap_slot(slot + 3u, D) * n.Ws, woff,
+                                          nw, b + 3 < B);
+                            stage_commit();
+                        }
                     }
                 }
                 // generator arrivals of this step (pure functions of source and time)
@@ -1008,7 +1112,8 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                     }
                     delivered += __popc(word);
                     if constexpr (S::deep)
-                        apply_word<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
+                        apply_word_staged<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t, pos_cur,
+                                             s_rec + (((b + 1) & 1) * 256 + threadIdx.x) * 2, pos_nxt);
                     else
                         apply_word_batched<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t, gen_cached_pos,
                                               gin[0].w, gin[0].meta);
@@ -1039,6 +1144,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             }
         }
         if (spk) {
+            pos_nxt = -1; // the post-synaptic pass below rewrites every record of this neuron
             // the out-list bounds the propagation reads after the last step
             if (!spk_steps)
                 asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(n.out_ptr + j)));
@@ -2190,6 +2296,11 @@ nbg_status nbg_create(const nbg_net_desc *d, const nbg_options *opt_in, nbg_engi
     chk(cudaEventCreate(&e->evr0), "event");
     chk(cudaEventCreate(&e->evr1), "event");
     chk(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, e->device), "SM count");
+    // the decay-table head in dynamic shared memory comes on top of the
+    // kernel's static staging arrays: above the 48 KiB a launch gets by default
+    chk(cudaFuncSetAttribute(reinterpret_cast<const void *>(e->update_kernel),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSharedDecayEntries * sizeof(float2))),
+        "update kernel shared memory");
     if (const char *rb = std::getenv("NBG_RASTER_BITMAP_WORDS")) {
         const long long v = std::atoll(rb);
         if (v > 0) e->raster_bitmap_words = (size_t)v;
