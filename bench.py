@@ -591,9 +591,9 @@ def bench_adjoint(args) -> dict:
     and forward + hand-written adjoint backward, per training step."""
     import torch
 
-    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+    from neuronbridge_gb300.adjoint import RECORD_BUDGET_BYTES, RecurrentLIF, poisson_inputs, record_bytes
 
-    model = RecurrentLIF()
+    model = RecurrentLIF()  # records every step's state (1.7 GB): no replay in the backward
     rates = torch.empty(256).uniform_(5.0, 50.0, generator=torch.Generator().manual_seed(5))
     x = poisson_inputs(rates, 1000, 128, dt=1.0, seed=5)
     labels = torch.randint(0, 10, (128,), generator=torch.Generator().manual_seed(6)).cuda()
@@ -628,7 +628,7 @@ def bench_adjoint(args) -> dict:
     gflop = 2 * 128 * (256 * 1024 + 1024 * 1024 + 1024 * 10) * 1000 / 1e9
     return _common(args, "training steps/s", 1e3 / t_ms, "steps/s", t_ms,
                    {"workload": "adjoint_rlif_b128_t1000", "batch": 128, "T": 1000, "n_rec": 1024,
-                    "checkpoint": 100},
+                    "segment": 100, "record": record_bytes(1000, 128, 1024) <= RECORD_BUDGET_BYTES},
                    forward_ms=f_ms, backward_ms=t_ms - f_ms, backward_over_forward=(t_ms - f_ms) / f_ms,
                    forward_tflops=gflop / f_ms)
 

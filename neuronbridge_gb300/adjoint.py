@@ -2,10 +2,14 @@
 
 ``RecurrentLIF`` runs T steps of the voltage-jump LIF recurrence of
 ``include/nbg_adjoint.h`` for a batch of B input sequences and returns the
-time-averaged leaky readout.  Its backward is not autograd: the forward saves
-the network state every ``checkpoint`` steps, and the backward replays each
-segment from its checkpoint (recording u_t, s_t, m_t, v_{t-1}) and runs the
-fused adjoint kernel in reverse time.
+time-averaged leaky readout.  Its backward is not autograd: the forward either records the state
+the adjoint reads (u_t, s_t, m_t, v_{t-1}) at every step, or saves the network
+state every ``checkpoint`` steps and lets the backward replay each segment from
+its checkpoint; the backward then runs the fused adjoint kernel in reverse
+time.  Recording is the default while the records fit in
+RECORD_BUDGET_BYTES (13 bytes per neuron, row and step: 1.7 GB at
+T = 1000, B = 128, N = 1024), which takes the replay, a third of the
+backward, off the training step.
 
 * Spiking mode: the forward (and the backward's replay) runs each checkpoint
   segment in one launch per row block: the input current of a step is the
@@ -190,13 +194,35 @@ def _fused_ok(p, B: int, N: int) -> bool:
     return FUSED_STEP and _tc_ok(p, B, N) and N >= 512
 
 
-def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out):
+# Largest state record (u, s, m, v_{t-1} of every step) a forward keeps by
+# default instead of checkpoints.
+RECORD_BUDGET_BYTES = 8 << 30
+
+
+def record_bytes(T: int, B: int, N: int) -> int:
+    """Bytes of the per-step record: u, v_{t-1} (FP32), m (uint8) for T steps
+    and s (FP32) for T + 1 (s_{-1} = 0 first)."""
+    return T * B * N * 9 + (T + 1) * B * N * 4
+
+
+def _record_buffers(T, B, N, dev):
+    """(U, S, M, VP): U[t] = u_t, S[t + 1] = s_t (S[0] = 0), M[t] = m_t,
+    VP[t] = v_{t-1}."""
+    S = torch.empty((T + 1, B, N), device=dev, dtype=torch.float32)
+    S[0].zero_()
+    return (torch.empty((T, B, N), device=dev, dtype=torch.float32), S,
+            torch.empty((T, B, N), device=dev, dtype=torch.uint8),
+            torch.empty((T, B, N), device=dev, dtype=torch.float32))
+
+
+def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck_ref, ck_s, z, out, rec=None):
     """Forward recurrence into caller-owned buffers: the checkpoints
-    ck_*[segment] (state entering each K-step segment), the readout
-    accumulator z and the output z W_out.  Launches only (no host sync), so it
-    runs eagerly or under CUDA graph capture alike.  With binary spikes the
-    recurrent product is the spike-driven gather-sum (one fused kernel per
-    step); with sigmoid spikes it is a GEMM."""
+    ck_*[segment] (state entering each K-step segment) or, with rec = (U, S,
+    M, VP) from _record_buffers, every step's state the adjoint reads; the
+    readout accumulator z and the output z W_out.  Launches only (no host
+    sync), so it runs eagerly or under CUDA graph capture alike.  With binary
+    spikes the recurrent product is the spike-driven gather-sum (one fused
+    kernel per segment); with sigmoid spikes it is a GEMM."""
     T, B, C = x.shape
     N = w_rec.shape[0]
     st = _stream()
@@ -212,19 +238,28 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
     I = torch.empty((B, N), device=x.device, dtype=torch.float32)
     for seg, t0 in enumerate(range(0, T, K)):
         t1 = min(T, t0 + K)
-        ck_v[seg].copy_(v)
-        ck_ref[seg].copy_(ref)
-        ck_s[seg].copy_(s_prev)
+        if rec is None:
+            ck_v[seg].copy_(v)
+            ck_ref[seg].copy_(ref)
+            ck_s[seg].copy_(s_prev)
         if sparse:  # the whole segment in one launch, inputs gathered in it
-            s_prev = sbuf[seg & 1]
-            lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, None, s_prev, None, None, None, z,
-                                 coef_dev[t0:t1], alpha, theta, p, t1 - t0, B, N, st)
+            if rec is None:
+                s_prev = sbuf[seg & 1]
+                lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, None, s_prev, None, None, None, z,
+                                     coef_dev[t0:t1], alpha, theta, p, t1 - t0, B, N, st)
+            else:
+                U, S, M, VP = rec
+                lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, S[t0 + 1], None, U[t0], M[t0], VP[t0], z,
+                                     coef_dev[t0:t1], alpha, theta, p, t1 - t0, B, N, st)
             continue
         xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
         for t in range(t0, t1):
-            s = sbuf[t & 1]
+            if rec is None:
+                s, u_t, m_t, vp_t = sbuf[t & 1], None, None, None
+            else:
+                s, u_t, m_t, vp_t = rec[1][t + 1], _ptr(rec[0][t]), _ptr(rec[2][t]), _ptr(rec[3][t])
             torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
-            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), None, None, None, _ptr(z),
+            _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), u_t, m_t, vp_t, _ptr(z),
                                                 float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
             s_prev = s
     _readout(lib, z, w_out, out, st)
@@ -238,11 +273,12 @@ def _readout(lib, z, w_out, out, st) -> None:
     _lib.check(lib.nbg_small_gemm(_ptr(z), N, 1, _ptr(w_out), O, 1, _ptr(out), B, O, N, st))
 
 
-def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref, ck_s, p, K, coef):
-    """Adjoint sweep: replay each segment from its checkpoint (recording
-    u_t, s_t, m_t, v_{t-1}), then run the fused adjoint step in reverse time.
-    Returns the gradients of (W_in, W_rec, W_out, alpha, theta).  Launches
-    only, like the forward body."""
+def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref, ck_s, p, K, coef, rec=None):
+    """Adjoint sweep over the K-step segments in reverse: each segment's
+    u_t, s_t, m_t, v_{t-1} from the forward's record (rec) or from a replay of
+    the segment from its checkpoint, then the fused adjoint step in reverse
+    time.  Returns the gradients of (W_in, W_rec, W_out, alpha, theta).
+    Launches only, like the forward body."""
     T, B, C = x.shape
     N = w_rec.shape[0]
     st = _stream()
@@ -259,15 +295,16 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     g_ext = torch.empty((B, N), device=x.device, dtype=torch.float32)
     I = torch.empty((B, N), device=x.device, dtype=torch.float32)
     L_max = min(K, T)
-    U = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
-    S = torch.empty((L_max + 1, B, N), device=x.device, dtype=torch.float32)  # S[0] = s_{t0-1}
-    M = torch.empty((L_max, B, N), device=x.device, dtype=torch.uint8)
-    VP = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
+    if rec is None:  # one segment's replay
+        U = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
+        S = torch.empty((L_max + 1, B, N), device=x.device, dtype=torch.float32)  # S[0] = s_{t0-1}
+        M = torch.empty((L_max, B, N), device=x.device, dtype=torch.uint8)
+        VP = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
     dI = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
     dI_next = torch.empty((B, N), device=x.device, dtype=torch.float32)
     have_next = False
     sparse = _sparse_ok(p, N)
-    lists = _SpikeLists(B, N, x.device) if sparse else None
+    lists = _SpikeLists(B, N, x.device) if sparse and rec is None else None
     tc = _tc_ok(p, B, N)
     fused = _fused_ok(p, B, N)
     if tc:
@@ -298,19 +335,22 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     for seg, t0 in reversed(segments):
         t1 = min(T, t0 + K)
         L = t1 - t0
-        v, ref = ck_v[seg].clone(), ck_ref[seg].clone()
-        S[0].copy_(ck_s[seg])
-        if sparse:  # replay the segment in one launch, recording u, m, v_{t-1} and s
-            lists.load(lib, S[0], B, N, st)
-            lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, S[1], None, U, M, VP, None, None, alpha, theta,
-                                 p, L, B, N, st)
-        else:
-            xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
-            for k in range(L):
-                torch.addmm(xi[k], S[k], w_rec, out=I)
-                _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
-                                                    _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha), _ptr(theta),
-                                                    ctypes.byref(p), B, N, st))
+        if rec is not None:  # the forward's record of the segment
+            U, S, M, VP = rec[0][t0:t1], rec[1][t0:t1 + 1], rec[2][t0:t1], rec[3][t0:t1]
+        else:  # replay the segment from its checkpoint, recording u, m, v_{t-1} and s
+            v, ref = ck_v[seg].clone(), ck_ref[seg].clone()
+            S[0].copy_(ck_s[seg])
+            if sparse:  # in one launch
+                lists.load(lib, S[0], B, N, st)
+                lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, S[1], None, U, M, VP, None, None, alpha,
+                                     theta, p, L, B, N, st)
+            else:
+                xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
+                for k in range(L):
+                    torch.addmm(xi[k], S[k], w_rec, out=I)
+                    _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
+                                                        _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha),
+                                                        _ptr(theta), ctypes.byref(p), B, N, st))
         for k in reversed(range(L)):
             t = t0 + k
             if fused:  # dI_{t+1} W_rec^T and the step t that consumes it, one launch
@@ -379,10 +419,11 @@ class _GraphPlan:
     thousands of small launches; replay removes their host cost).  Inputs are
     copied into the static buffers before a replay and results cloned out, so
     callers never alias graph memory.  Keyed by shape, checkpoint interval,
-    readout coefficients, LIF parameters and the parameters' storage; in-place
-    optimiser updates keep the storage, so one plan serves a training run."""
+    record mode, readout coefficients, LIF parameters and the parameters'
+    storage; in-place optimiser updates keep the storage, so one plan serves a
+    training run."""
 
-    def __init__(self, x, w_in, w_rec, w_out, alpha, theta, p, K, coef):
+    def __init__(self, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, record):
         T, B, C = x.shape
         N = w_rec.shape[0]
         nseg = (T + K - 1) // K
@@ -390,15 +431,17 @@ class _GraphPlan:
         self.params = (w_in, w_rec, w_out, alpha, theta)
         self.p, self.K, self.coef = p, K, coef
         self.x = torch.empty_like(x)
-        self.ck_v = torch.empty((nseg, B, N), device=dev, dtype=torch.float32)
-        self.ck_ref = torch.empty((nseg, B, N), device=dev, dtype=torch.int32)
-        self.ck_s = torch.empty((nseg, B, N), device=dev, dtype=torch.float32)
+        self.rec = _record_buffers(T, B, N, dev) if record else None
+        ck = 0 if record else nseg
+        self.ck_v = torch.empty((ck, B, N), device=dev, dtype=torch.float32)
+        self.ck_ref = torch.empty((ck, B, N), device=dev, dtype=torch.int32)
+        self.ck_s = torch.empty((ck, B, N), device=dev, dtype=torch.float32)
         self.z = torch.empty((B, N), device=dev, dtype=torch.float32)
         self.out = torch.empty((B, w_out.shape[1]), device=dev, dtype=torch.float32)
         self.gy = torch.empty((B, w_out.shape[1]), device=dev, dtype=torch.float32)
         self.fwd = self.bwd = None
         self.grads = None
-        self.owner = None  # the forward whose x and checkpoints the buffers hold
+        self.owner = None  # the forward whose x and checkpoints (or record) the buffers hold
 
     @staticmethod
     def _capture(fn):
@@ -419,7 +462,7 @@ class _GraphPlan:
             w_in, w_rec, w_out, alpha, theta = self.params
             self.fwd, _ = self._capture(lambda: _forward_body(
                 lib, self.x, w_in, w_rec, w_out, alpha, theta, self.p, self.K, self.coef, self.ck_v, self.ck_ref,
-                self.ck_s, self.z, self.out))
+                self.ck_s, self.z, self.out, self.rec))
         self.fwd.replay()
         self.owner = object()
         return self.owner
@@ -428,17 +471,20 @@ class _GraphPlan:
         lib = _bind()
         if owner is not self.owner:  # another forward ran since: restore this one's inputs
             self.x.copy_(x)
-            self.ck_v.copy_(saved[0])
-            self.ck_ref.copy_(saved[1])
-            self.ck_s.copy_(saved[2])
-            self.z.copy_(saved[3])
+            if self.rec is not None:  # run its forward again: the same launches give the same record
+                self.fwd.replay()
+            else:
+                self.ck_v.copy_(saved[0])
+                self.ck_ref.copy_(saved[1])
+                self.ck_s.copy_(saved[2])
+                self.z.copy_(saved[3])
             self.owner = owner
         self.gy.copy_(gy)
         if self.bwd is None:
             w_in, w_rec, w_out, alpha, theta = self.params
             self.bwd, self.grads = self._capture(lambda: _backward_body(
                 lib, self.gy, self.x, w_in, w_rec, w_out, alpha, theta, self.z, self.ck_v, self.ck_ref, self.ck_s,
-                self.p, self.K, self.coef))
+                self.p, self.K, self.coef, self.rec))
         self.bwd.replay()
         _check_tc(self.grads[5])
         return tuple(g.clone() for g in self.grads[:5])
@@ -457,18 +503,23 @@ class _Recurrence(torch.autograd.Function):
         if plan is not None:
             ctx.owner = plan.forward(x)
             z = plan.z.clone()
-            saved = (plan.ck_v.clone(), plan.ck_ref.clone(), plan.ck_s.clone()) if cfg["needs_grad"] else ()
-            ctx.ck = saved
+            keep = cfg["needs_grad"] and plan.rec is None
+            ctx.ck = (plan.ck_v.clone(), plan.ck_ref.clone(), plan.ck_s.clone()) if keep else ()
+            ctx.rec = None
             ctx.save_for_backward(x, w_in, w_rec, w_out, alpha, theta, z)
             return plan.out.clone()
-        ck_v = torch.empty((nseg, B, N), device=x.device, dtype=torch.float32)
-        ck_ref = torch.empty((nseg, B, N), device=x.device, dtype=torch.int32)
-        ck_s = torch.empty((nseg, B, N), device=x.device, dtype=torch.float32)
+        record = cfg["record"]
+        ck = 0 if record else nseg
+        ck_v = torch.empty((ck, B, N), device=x.device, dtype=torch.float32)
+        ck_ref = torch.empty((ck, B, N), device=x.device, dtype=torch.int32)
+        ck_s = torch.empty((ck, B, N), device=x.device, dtype=torch.float32)
+        rec = _record_buffers(T, B, N, x.device) if record else None
         z = torch.empty((B, N), device=x.device, dtype=torch.float32)
         out = torch.empty((B, w_out.shape[1]), device=x.device, dtype=torch.float32)
         _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, cfg["params"], K, cfg["coef"], ck_v, ck_ref, ck_s,
-                      z, out)
+                      z, out, rec)
         ctx.ck = (ck_v, ck_ref, ck_s)
+        ctx.rec = rec if cfg["needs_grad"] else None
         ctx.save_for_backward(x, w_in, w_rec, w_out, alpha, theta, z)
         return out
 
@@ -482,19 +533,25 @@ class _Recurrence(torch.autograd.Function):
             grads = plan.backward(ctx.owner, gy, x, ctx.ck + (z,))
         else:
             *grads, err = _backward_body(_bind(), gy, x, w_in, w_rec, w_out, alpha, theta, z, *ctx.ck, cfg["params"],
-                                         cfg["checkpoint"], cfg["coef"])
+                                         cfg["checkpoint"], cfg["coef"], ctx.rec)
             _check_tc(err)
         return (None, *grads, None)
 
 
 class RecurrentLIF(torch.nn.Module):
     """n_in Poisson channels -> n_rec recurrent voltage-jump LIF -> n_out leaky
-    readout; ``forward(x)`` returns the time-averaged readout (B x n_out)."""
+    readout; ``forward(x)`` returns the time-averaged readout (B x n_out).
+
+    ``checkpoint``: the segment length of the launches (and of the replay);
+    ``record``: keep every step's state for the backward (True), replay
+    segments from checkpoints (False), or record while ``record_bytes`` fits
+    in RECORD_BUDGET_BYTES (None)."""
 
     def __init__(self, n_in: int = 256, n_rec: int = 1024, n_out: int = 10, *, dt: float = 1.0, tau: float = 20.0,
                  v_rest: float = -65.0, v_reset: float = -65.0, v_th: float = -50.0, t_ref_ms: float = 2.0,
                  tau_out: float = 20.0, slope: float = 10.0, smooth: bool = False, checkpoint: int = 100,
-                 weight_scale: float = 1.0, seed: int = 5, device: str = "cuda", use_graphs: bool = True):
+                 record: bool | None = None, weight_scale: float = 1.0, seed: int = 5, device: str = "cuda",
+                 use_graphs: bool = True):
         super().__init__()
         g = torch.Generator().manual_seed(seed)
         init = lambda *shape: (torch.randn(*shape, generator=g, dtype=torch.float64) * weight_scale /
@@ -506,6 +563,7 @@ class RecurrentLIF(torch.nn.Module):
         self.theta = torch.nn.Parameter(torch.full((n_rec,), v_th, device=device))
         self.params = GradParams(v_rest, v_reset, slope, int(round(t_ref_ms / dt)), int(bool(smooth)))
         self.dt, self.tau_out, self.checkpoint = dt, tau_out, int(checkpoint)
+        self.record = record
         self.use_graphs = bool(use_graphs)
         self._plans = {}
 
@@ -514,16 +572,19 @@ class RecurrentLIF(torch.nn.Module):
         a_out = math.exp(-self.dt / self.tau_out)
         coef = readout_coefficients(T, a_out)
         x = x.contiguous()
-        cfg = {"params": self.params, "checkpoint": self.checkpoint, "coef": coef,
+        record = self.record
+        if record is None:
+            record = record_bytes(T, x.shape[1], self.w_rec.shape[0]) <= RECORD_BUDGET_BYTES
+        cfg = {"params": self.params, "checkpoint": self.checkpoint, "coef": coef, "record": bool(record),
                "needs_grad": torch.is_grad_enabled() and any(q.requires_grad for q in self.parameters())}
         if self.use_graphs:
-            key = (tuple(x.shape), str(x.device), self.checkpoint, coef.tobytes(), bytes(self.params),
+            key = (tuple(x.shape), str(x.device), self.checkpoint, bool(record), coef.tobytes(), bytes(self.params),
                    tuple(q.data_ptr() for q in self.parameters()))
             plan = self._plans.get(key)
             if plan is None:
                 self._plans.clear()
                 plan = self._plans[key] = _GraphPlan(x, self.w_in, self.w_rec, self.w_out, self.alpha, self.theta,
-                                                     self.params, self.checkpoint, coef)
+                                                     self.params, self.checkpoint, coef, bool(record))
             cfg["plan"] = plan
         return _Recurrence.apply(x, self.w_in, self.w_rec, self.w_out, self.alpha, self.theta, cfg)
 

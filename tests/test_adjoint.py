@@ -136,12 +136,14 @@ def test_graph_replay_matches_eager_with_ragged_segment_and_sgd_steps():
 
 
 @pytest.mark.gpu
-def test_graph_plan_backward_after_interleaved_forwards():
+@pytest.mark.parametrize("record", [False, True])
+def test_graph_plan_backward_after_interleaved_forwards(record):
     """Two forwards before either backward: each backward restores its own
-    inputs and checkpoints into the plan's static buffers."""
+    inputs and checkpoints into the plan's static buffers (replay mode) or
+    runs its forward again to rebuild the record (record mode)."""
     from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
 
-    model = RecurrentLIF(**KW, **SPIKING)
+    model = RecurrentLIF(record=record, **KW, **SPIKING)
     xs = [poisson_inputs(torch.linspace(40.0, 400.0, KW["n_in"]), T, B, dt=1.0, seed=s) for s in (5, 6)]
     labels = torch.randint(0, KW["n_out"], (B,), generator=torch.Generator().manual_seed(2)).cuda()
     alone = [_grads(model, x, labels)[1] for x in xs]
@@ -151,6 +153,33 @@ def test_graph_plan_backward_after_interleaved_forwards():
         model.zero_grad(set_to_none=True)
         loss.backward()
         _close([p.grad for p in _params(model)], want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graphs", [False, True])
+def test_recorded_state_gradients_equal_replayed(graphs):
+    """Recording every step's state in the forward and replaying segments
+    from checkpoints in the backward run the same kernels on the same values:
+    the loss and all five gradients are bitwise equal.  T = 70 with segments
+    of 20 leaves a ragged last segment; N = 512 takes the fused tensor-core
+    adjoint step."""
+    from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
+
+    kw = dict(n_in=64, n_rec=512, n_out=5, checkpoint=20, seed=11)
+    x = poisson_inputs(torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0, 70, 128, dt=1.0, seed=3)
+    labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
+    out = [_grads(RecurrentLIF(record=r, use_graphs=graphs, **kw, **SPIKING), x, labels) for r in (False, True)]
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert torch.equal(a, b)
+
+
+def test_record_mode_default_follows_budget():
+    from neuronbridge_gb300 import adjoint
+
+    assert adjoint.record_bytes(1000, 128, 1024) == 1000 * 128 * 1024 * 9 + 1001 * 128 * 1024 * 4
+    assert adjoint.record_bytes(1000, 128, 1024) <= adjoint.RECORD_BUDGET_BYTES  # the benchmark's size records
+    assert adjoint.record_bytes(10000, 512, 4096) > adjoint.RECORD_BUDGET_BYTES  # this one replays
 
 
 def test_reference_dynamics_gradcheck_cpu():
@@ -287,21 +316,22 @@ def test_segment_gather_equals_ascending_input_sum(binary):
 
 
 @pytest.mark.gpu
-def test_fused_adjoint_step_equals_two_launch_form(monkeypatch):
-    """N = 512, B = 128, spiking mode: each backward step as one launch
+@pytest.mark.parametrize("n_rec", [512, 1024])
+def test_fused_adjoint_step_equals_two_launch_form(monkeypatch, n_rec):
+    """N = 512 and 1024, B = 128, spiking mode: each backward step as one launch
     (nbg_lif_adjoint_step_fused, split-K partials reduced through distributed
     shared memory) gives the same gradients, bit for bit, as the product and
     the step as two launches, and stays within the FP64 tolerance."""
     from neuronbridge_gb300 import adjoint
     from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
 
-    kw = dict(n_in=64, n_rec=512, n_out=5, checkpoint=20, seed=11)
+    kw = dict(n_in=64, n_rec=n_rec, n_out=5, checkpoint=20, seed=11)
     torch.manual_seed(0)
     model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, **kw, **SPIKING)
     rates = torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0
     x = poisson_inputs(rates, T, 128, dt=1.0, seed=3)
     labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
-    assert adjoint._fused_ok(model.params, 128, 512)
+    assert adjoint._fused_ok(model.params, 128, n_rec)
     loss_f, fused = _grads(model, x, labels)
     monkeypatch.setattr(adjoint, "FUSED_STEP", False)
     loss_u, unfused = _grads(model, x, labels)
