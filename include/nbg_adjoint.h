@@ -114,9 +114,16 @@ nbg_status nbg_adjoint_rec_grad(const void *w_hi, const void *w_lo, const void *
 /* One adjoint step t in one launch, N >= 512 (a multiple of 128), B = 128:
  * the recurrent term dI_{t+1} W_rec^T on the tensor cores (as
  * nbg_adjoint_rec_grad, from dI_hi_in / dI_lo_in) and the step of
- * nbg_lif_adjoint_step_split on it, which writes dI_t (FP32 into dI, the
- * split BF16 operand into dI_hi_out / dI_lo_out; the in and out operand
- * buffers must differ).  The split-K partials never leave the chip: the 8
+ * nbg_lif_adjoint_step_split on it, which writes dI_t: the split BF16
+ * operand of the next step's product into dI_hi_out / dI_lo_out (the in and
+ * out operand buffers must differ), FP32 into dI unless dI is NULL, and,
+ * unless dT_hi is NULL, dI_t^T split into dT_hi / dT_lo as columns
+ * k_off .. k_off + 127 of the N x k_cols blocked matrix that
+ * nbg_adjoint_blocked_t would make of it (k_off a multiple of 128, k_cols
+ * of 64): the weight gradients' operand without a transpose.  With dI_hi_in
+ * / dI_lo_in all zeros (the last step of the run) the results equal
+ * nbg_lif_adjoint_step_split's without a recurrent term (a zero may differ
+ * in sign).  The split-K partials never leave the chip: the 8
  * CTAs of a cluster that share a 128-row tile reduce them through
  * distributed shared memory, in the same order as the two-launch form, so
  * the results are identical to it.  A bounded wait that gives up sets
@@ -126,8 +133,8 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
                                       void *dI_hi_out, void *dI_lo_out, const float *g_read, float c_t,
                                       const float *u, const float *s, const uint8_t *m, const float *vprev,
                                       float *lam_v, float *dI, float *g_theta, float *g_alpha, const float *alpha,
-                                      const float *theta, const nbg_lif_grad_params *p, int B, int N, int *err,
-                                      void *stream);
+                                      const float *theta, const nbg_lif_grad_params *p, int B, int N, void *dT_hi,
+                                      void *dT_lo, int64_t k_off, int64_t k_cols, int *err, void *stream);
 
 /* The recurrent weight gradient of a checkpoint segment on the tensor cores,
  * dW_rec += sum over its L steps of S_{t-1}^T dI_t, in three calls:

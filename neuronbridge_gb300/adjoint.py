@@ -64,7 +64,8 @@ _SIG = {
                                    [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp]),
     "nbg_adjoint_rec_grad": (ctypes.c_int, [_vp] * 5 + [ctypes.c_int] * 3 + [_vp, _vp]),
     "nbg_lif_adjoint_step_fused": (ctypes.c_int, [_vp] * 7 + [ctypes.c_float] + [_vp] * 10 +
-                                   [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp, _vp]),
+                                   [ctypes.POINTER(GradParams), ctypes.c_int, ctypes.c_int, _vp, _vp,
+                                    ctypes.c_int64, ctypes.c_int64, _vp, _vp]),
     "nbg_adjoint_blocked_t": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp,
                                              _vp]),
     "nbg_small_gemm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp,
@@ -276,61 +277,82 @@ def _readout(lib, z, w_out, out, st) -> None:
 def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref, ck_s, p, K, coef, rec=None):
     """Adjoint sweep over the K-step segments in reverse: each segment's
     u_t, s_t, m_t, v_{t-1} from the forward's record (rec) or from a replay of
-    the segment from its checkpoint, then the fused adjoint step in reverse
-    time.  Returns the gradients of (W_in, W_rec, W_out, alpha, theta).
-    Launches only, like the forward body."""
+    the segment from its checkpoint, then the adjoint step in reverse time and
+    the weight gradients (per segment, or once over the whole run when the
+    state is recorded).  Returns the gradients of (W_in, W_rec, W_out, alpha,
+    theta).  Launches only, like the forward body."""
     T, B, C = x.shape
     N = w_rec.shape[0]
+    dev = x.device
     st = _stream()
     O = w_out.shape[1]
-    g_read = torch.empty((B, N), device=x.device, dtype=torch.float32)  # gy W_out^T
-    g_w_out = torch.empty((N, O), device=x.device, dtype=torch.float32)  # z^T gy
+    g_read = torch.empty((B, N), device=dev, dtype=torch.float32)  # gy W_out^T
+    g_w_out = torch.empty((N, O), device=dev, dtype=torch.float32)  # z^T gy
     _lib.check(lib.nbg_small_gemm(_ptr(gy), O, 1, _ptr(w_out), 1, O, _ptr(g_read), B, N, O, st))
     _lib.check(lib.nbg_small_gemm(_ptr(z), 1, N, _ptr(gy), O, 1, _ptr(g_w_out), N, O, B, st))
     g_w_in = torch.zeros_like(w_in)
     g_w_rec = torch.zeros_like(w_rec)
-    lam_v = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-    g_theta = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-    g_alpha = torch.zeros((B, N), device=x.device, dtype=torch.float32)
-    g_ext = torch.empty((B, N), device=x.device, dtype=torch.float32)
-    I = torch.empty((B, N), device=x.device, dtype=torch.float32)
+    lam_v = torch.zeros((B, N), device=dev, dtype=torch.float32)
+    g_theta = torch.zeros((B, N), device=dev, dtype=torch.float32)
+    g_alpha = torch.zeros((B, N), device=dev, dtype=torch.float32)
+    g_ext = torch.empty((B, N), device=dev, dtype=torch.float32)
+    I = torch.empty((B, N), device=dev, dtype=torch.float32)
     L_max = min(K, T)
     if rec is None:  # one segment's replay
-        U = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
-        S = torch.empty((L_max + 1, B, N), device=x.device, dtype=torch.float32)  # S[0] = s_{t0-1}
-        M = torch.empty((L_max, B, N), device=x.device, dtype=torch.uint8)
-        VP = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
-    dI = torch.empty((L_max, B, N), device=x.device, dtype=torch.float32)
-    dI_next = torch.empty((B, N), device=x.device, dtype=torch.float32)
+        U = torch.empty((L_max, B, N), device=dev, dtype=torch.float32)
+        S = torch.empty((L_max + 1, B, N), device=dev, dtype=torch.float32)  # S[0] = s_{t0-1}
+        M = torch.empty((L_max, B, N), device=dev, dtype=torch.uint8)
+        VP = torch.empty((L_max, B, N), device=dev, dtype=torch.float32)
     have_next = False
     sparse = _sparse_ok(p, N)
-    lists = _SpikeLists(B, N, x.device) if sparse and rec is None else None
+    lists = _SpikeLists(B, N, dev) if sparse and rec is None else None
     tc = _tc_ok(p, B, N)
     fused = _fused_ok(p, B, N)
+    # the fused step writes dI^T for the weight gradients itself (no FP32 dI,
+    # no transpose); the other forms keep dI in FP32
+    dI = None if fused else torch.empty((L_max, B, N), device=dev, dtype=torch.float32)
+    dI_next = None if fused else torch.empty((B, N), device=dev, dtype=torch.float32)
     if tc:
-        w_hi = torch.empty(N * N, device=x.device, dtype=torch.bfloat16)
-        w_lo = torch.empty(N * N, device=x.device, dtype=torch.bfloat16)
+        w_hi = torch.empty(N * N, device=dev, dtype=torch.bfloat16)
+        w_lo = torch.empty(N * N, device=dev, dtype=torch.bfloat16)
         # the split BF16 operand dI: two buffers in the fused form (a step
-        # reads one while writing the other), else one
-        d_hi = [torch.empty(B * N, device=x.device, dtype=torch.bfloat16) for _ in range(2 if fused else 1)]
-        d_lo = [torch.empty(B * N, device=x.device, dtype=torch.bfloat16) for _ in range(2 if fused else 1)]
+        # reads one while writing the other; the run's last step reads zeros),
+        # else one
+        d_hi = [torch.zeros(B * N, device=dev, dtype=torch.bfloat16) for _ in range(2 if fused else 1)]
+        d_lo = [torch.zeros(B * N, device=dev, dtype=torch.bfloat16) for _ in range(2 if fused else 1)]
         split = min(TC_SPLIT, N // 64)
-        g_parts = None if fused else torch.empty((split, B, N), device=x.device, dtype=torch.float32)
-        tc_err = torch.zeros(1, device=x.device, dtype=torch.int32)
+        g_parts = None if fused else torch.empty((split, B, N), device=dev, dtype=torch.float32)
+        tc_err = torch.zeros(1, device=dev, dtype=torch.int32)
         _lib.check(lib.nbg_adjoint_rec_prepare(_ptr(w_rec), _ptr(w_hi), _ptr(w_lo), N, st))
     # weight gradients on the tensor cores: the product's column operand (S^T,
-    # X^T) is padded with zero rows to a multiple of 256
-    tc_w = tc_in = tc
-    if tc_w:
-        kk_max = L_max * B
+    # X^T) is padded with zero rows to a multiple of 256; with the state
+    # recorded they run once, over every (step, row) pair of the run
+    whole = fused and rec is not None
+    if tc:
+        kk_max = (T if whole else L_max) * B
         N256, C256 = -(-N // 256) * 256, -(-C // 256) * 256
-        dT_hi = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
-        dT_lo = torch.empty(N * kk_max, device=x.device, dtype=torch.bfloat16)
-        sT = torch.empty(N256 * kk_max, device=x.device, dtype=torch.bfloat16)
-        w_part = torch.empty(max(WGRAD_SPLIT * N256 * N, WGRAD_IN_SPLIT * C256 * N), device=x.device,
+        dT_hi = torch.empty(N * kk_max, device=dev, dtype=torch.bfloat16)
+        dT_lo = torch.empty(N * kk_max, device=dev, dtype=torch.bfloat16)
+        sT = torch.empty(N256 * kk_max, device=dev, dtype=torch.bfloat16)
+        w_part = torch.empty(max(WGRAD_SPLIT * N256 * N, WGRAD_IN_SPLIT * C256 * N), device=dev,
                              dtype=torch.float32)
-        xT_hi = torch.empty(C256 * kk_max, device=x.device, dtype=torch.bfloat16)
-        xT_lo = torch.empty(C256 * kk_max, device=x.device, dtype=torch.bfloat16)
+        xT_hi = torch.empty(C256 * kk_max, device=dev, dtype=torch.bfloat16)
+        xT_lo = torch.empty(C256 * kk_max, device=dev, dtype=torch.bfloat16)
+
+    def wgrad(s_rows, x_rows, L):
+        """dW_rec += S^T dI and dW_in += X^T dI over L steps, dI^T in dT."""
+        kk = L * B
+        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(s_rows), L, B, N, N256, _ptr(sT), None, st))
+        ws = min(WGRAD_SPLIT, kk // 64)
+        _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(sT), None, N, N256, kk, _ptr(w_part), ws,
+                                         _ptr(tc_err), st))
+        _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_rec), _ptr(w_part), ws, N * N, N256 * N, st))
+        ws = min(WGRAD_IN_SPLIT, kk // 64)
+        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x_rows), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), st))
+        _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(xT_hi), _ptr(xT_lo), N, C256, kk,
+                                         _ptr(w_part), ws, _ptr(tc_err), st))
+        _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_in), _ptr(w_part), ws, C * N, C256 * N, st))
+
     segments = list(enumerate(range(0, T, K)))
     for seg, t0 in reversed(segments):
         t1 = min(T, t0 + K)
@@ -353,20 +375,14 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                                                         _ptr(theta), ctypes.byref(p), B, N, st))
         for k in reversed(range(L)):
             t = t0 + k
-            if fused:  # dI_{t+1} W_rec^T and the step t that consumes it, one launch
+            if fused:  # dI_{t+1} W_rec^T (zero at the run's last step) and step t, one launch
                 cur, nxt = t & 1, (t + 1) & 1
-                if have_next:
-                    _lib.check(lib.nbg_lif_adjoint_step_fused(
-                        _ptr(w_hi), _ptr(w_lo), _ptr(d_hi[nxt]), _ptr(d_lo[nxt]), _ptr(d_hi[cur]), _ptr(d_lo[cur]),
-                        _ptr(g_read), float(coef[t]), _ptr(U[k]), _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]),
-                        _ptr(lam_v), _ptr(dI[k]), _ptr(g_theta), _ptr(g_alpha), _ptr(alpha), _ptr(theta),
-                        ctypes.byref(p), B, N, _ptr(tc_err), st))
-                else:  # the last step of the run: no recurrent term yet
-                    _lib.check(lib.nbg_lif_adjoint_step_split(
-                        None, split, _ptr(g_read), float(coef[t]), _ptr(U[k]), _ptr(S[k + 1]), _ptr(M[k]),
-                        _ptr(VP[k]), _ptr(lam_v), _ptr(dI[k]), _ptr(d_hi[cur]), _ptr(d_lo[cur]), _ptr(g_theta),
-                        _ptr(g_alpha), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
-                have_next = True
+                k_off, k_cols = (t * B, T * B) if whole else (k * B, L * B)
+                _lib.check(lib.nbg_lif_adjoint_step_fused(
+                    _ptr(w_hi), _ptr(w_lo), _ptr(d_hi[nxt]), _ptr(d_lo[nxt]), _ptr(d_hi[cur]), _ptr(d_lo[cur]),
+                    _ptr(g_read), float(coef[t]), _ptr(U[k]), _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]),
+                    _ptr(lam_v), None, _ptr(g_theta), _ptr(g_alpha), _ptr(alpha), _ptr(theta), ctypes.byref(p), B,
+                    N, _ptr(dT_hi), _ptr(dT_lo), k_off, k_cols, _ptr(tc_err), st))
                 continue
             if tc:  # g_parts holds dI_{t+1} W_rec^T from the previous iteration
                 _lib.check(lib.nbg_lif_adjoint_step_split(
@@ -386,24 +402,19 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                                                 _ptr(dI[k]), _ptr(g_theta), _ptr(g_alpha), _ptr(alpha),
                                                 _ptr(theta), ctypes.byref(p), B, N, st))
             have_next = True
-        if tc_w:
-            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, N, _ptr(dT_hi), _ptr(dT_lo), st))
-            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(S), L, B, N, N256, _ptr(sT), None, st))
-            ws = min(WGRAD_SPLIT, L * B // 64)
-            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(sT), None, N, N256, L * B, _ptr(w_part),
-                                             ws, _ptr(tc_err), st))
-            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_rec), _ptr(w_part), ws, N * N, N256 * N, st))
+        if whole:
+            continue
+        if tc:
+            if not fused:  # dI^T from the FP32 dI
+                _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, N, _ptr(dT_hi), _ptr(dT_lo), st))
+            wgrad(S, x[t0:t1], L)
         else:
             g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
-        if tc_w and tc_in:
-            ws = min(WGRAD_IN_SPLIT, L * B // 64)
-            _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x[t0:t1]), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), st))
-            _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(xT_hi), _ptr(xT_lo), N, C256, L * B,
-                                             _ptr(w_part), ws, _ptr(tc_err), st))
-            _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_in), _ptr(w_part), ws, C * N, C256 * N, st))
-        else:
             g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
-        dI_next.copy_(dI[0])
+        if dI_next is not None:
+            dI_next.copy_(dI[0])
+    if whole:  # the whole run's weight gradients at once
+        wgrad(rec[1], x, T)
     return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), (tc_err if tc else None)
 
 

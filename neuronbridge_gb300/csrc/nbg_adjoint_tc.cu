@@ -245,9 +245,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 // r reduces batch rows [16 r, 16 r + 16) of the tile over the partials of
 // ranks 0..7 in order (read through distributed shared memory) -- the sum
 // k_lif_adj_split forms from g_parts, so the result is the same bit for bit
-// -- and runs the adjoint step on those elements, writing dI_t in FP32 and
-// as the split BF16 operand of the next step's product into the other of
-// two buffers (the next launch reads this one while writing its own).  A
+// -- and runs the adjoint step on those elements, writing dI_t as the split
+// BF16 operand of the next step's product into the other of two buffers
+// (the next launch reads this one while writing its own), in FP32 (when dI
+// is given) and as the split BF16 operand of the weight gradients (when dT_hi
+// is given: dI^T, row i, column k_off + b of a k_cols-column blocked matrix,
+// eight consecutive b of one i per 16-byte store).  A
 // second cluster barrier keeps every CTA's shared memory alive until its
 // peers have read it.  Waits on mbarriers are bounded as in k_adj_umma; a
 // CTA that gives up still takes part in both cluster barriers, and the
@@ -261,7 +264,8 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     float c_t, const float *__restrict__ u, const float *__restrict__ s, const unsigned char *__restrict__ m,
     const float *__restrict__ vprev, float *__restrict__ lam_v, float *__restrict__ dI, float *__restrict__ g_theta,
     float *__restrict__ g_alpha, const float *__restrict__ alpha, const float *__restrict__ theta,
-    nbg_lif_grad_params p, int n, int *__restrict__ err) {
+    nbg_lif_grad_params p, int n, __nv_bfloat16 *__restrict__ dT_hi, __nv_bfloat16 *__restrict__ dT_lo,
+    long long k_off, long long k_cols, int *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(stages + kAdjStages * kAdjStageBytes);
@@ -355,8 +359,9 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     }
     __syncwarp();
     asm volatile("griddepcontrol.wait;" ::: "memory"); // the previous step's writes are visible
-    // this thread's share of the adjoint step: batch rows 16 ks + bsub + 2 k
-    // of column i.  Its operands are loaded now, while the products run.
+    // this thread's share of the adjoint step: batch rows 16 ks + 8 bsub + k
+    // of column i (eight consecutive rows: one 16-byte store of dI^T).  Its
+    // operands are loaded now, while the products run.
     const int il = threadIdx.x & 127, bsub = threadIdx.x >> 7;
     const int i = mt * kAdjM + il;
     constexpr int kRows = 8;
@@ -364,7 +369,7 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     unsigned char op_m[kRows];
 #pragma unroll
     for (int k = 0; k < kRows; ++k) {
-        const size_t idx = (size_t)(16 * ks + bsub + 2 * k) * n + i;
+        const size_t idx = (size_t)(16 * ks + 8 * bsub + k) * n + i;
         op_u[k] = u[idx];
         op_s[k] = s[idx];
         op_lv[k] = lam_v[idx];
@@ -404,7 +409,7 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
         float x[kRows][kAdjCluster];
 #pragma unroll
         for (int k = 0; k < kRows; ++k) {
-            const uint32_t off = local + (uint32_t)(((16 * ks + bsub + 2 * k) * kAdjM + il) * 4);
+            const uint32_t off = local + (uint32_t)(((16 * ks + 8 * bsub + k) * kAdjM + il) * 4);
 #pragma unroll
             for (int r = 0; r < kAdjCluster; ++r) {
                 uint32_t ra;
@@ -412,9 +417,10 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
                 asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x[k][r]) : "r"(ra));
             }
         }
+        uint32_t t_hi[kRows / 2], t_lo[kRows / 2]; // dI^T of the eight rows, split, packed in pairs
 #pragma unroll
         for (int k = 0; k < kRows; ++k) {
-            const int b = 16 * ks + bsub + 2 * k;
+            const int b = 16 * ks + 8 * bsub + k;
             float ge = x[k][0];
 #pragma unroll
             for (int r = 1; r < kAdjCluster; ++r) ge = ge + x[k][r];
@@ -425,12 +431,28 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
             gs = gs + ge;
             const float gu = gs * dsdu + lv * (1.0f - ss);
             const float gm = op_m[k] ? gu : 0.0f;
-            dI[idx] = gm;
+            if (dI) dI[idx] = gm;
             const size_t o = blocked_index(b, i, n);
-            split_bf16(gm, d_hi_out[o], d_lo_out[o]);
+            __nv_bfloat16 h, l;
+            split_bf16(gm, h, l);
+            d_hi_out[o] = h;
+            d_lo_out[o] = l;
+            const uint32_t hb = __bfloat16_as_ushort(h), lb = __bfloat16_as_ushort(l);
+            if (k & 1) {
+                t_hi[k >> 1] |= hb << 16;
+                t_lo[k >> 1] |= lb << 16;
+            } else {
+                t_hi[k >> 1] = hb;
+                t_lo[k >> 1] = lb;
+            }
             lam_v[idx] = gm * (1.0f - al);
             g_theta[idx] = op_gt[k] - gs * dsdu;
             g_alpha[idx] = op_ga[k] + gm * (p.v_rest - op_vp[k]);
+        }
+        if (dT_hi) {
+            const size_t o = blocked_index(i, (int)(k_off + 16 * ks + 8 * bsub), (int)k_cols);
+            reinterpret_cast<uint4 *>(dT_hi + o)[0] = make_uint4(t_hi[0], t_hi[1], t_hi[2], t_hi[3]);
+            reinterpret_cast<uint4 *>(dT_lo + o)[0] = make_uint4(t_lo[0], t_lo[1], t_lo[2], t_lo[3]);
         }
     }
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
@@ -689,14 +711,18 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
                                       void *dI_hi_out, void *dI_lo_out, const float *g_read, float c_t,
                                       const float *u, const float *s, const uint8_t *m, const float *vprev,
                                       float *lam_v, float *dI, float *g_theta, float *g_alpha, const float *alpha,
-                                      const float *theta, const nbg_lif_grad_params *p, int B, int N, int *err,
-                                      void *stream) {
+                                      const float *theta, const nbg_lif_grad_params *p, int B, int N, void *dT_hi,
+                                      void *dT_lo, int64_t k_off, int64_t k_cols, int *err, void *stream) {
     if (!w_hi || !w_lo || !dI_hi_in || !dI_lo_in || !dI_hi_out || !dI_lo_out || !g_read || !u || !s || !m ||
-        !vprev || !lam_v || !dI || !g_theta || !g_alpha || !alpha || !theta || !p || !err || !adj_shape_ok(B, N) ||
+        !vprev || !lam_v || !g_theta || !g_alpha || !alpha || !theta || !p || !err || !adj_shape_ok(B, N) ||
         N / kKChunk < kAdjCluster || dI_hi_in == dI_hi_out || dI_lo_in == dI_lo_out)
         return nbg_fail(NBG_ERR_INVALID, "nbg_lif_adjoint_step_fused: bad arguments (B must be %d, N a multiple of %d "
                         "and at least %d, distinct in and out operand buffers)", kAdjN, kAdjM,
                         kAdjCluster * kKChunk);
+    if (dT_hi && (!dT_lo || k_off < 0 || k_off % kAdjN || k_cols % kKChunk || k_off + kAdjN > k_cols ||
+                  k_cols > 0x7fffffff))
+        return nbg_fail(NBG_ERR_INVALID, "nbg_lif_adjoint_step_fused: dT needs dT_lo, k_off a multiple of %d with "
+                        "k_off + %d <= k_cols, k_cols a multiple of %d below 2^31", kAdjN, kAdjN, kKChunk);
     static bool attr_set = false;
     if (!attr_set) {
         NBG_CUDA(cudaFuncSetAttribute(k_adj_step_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmemBytes));
@@ -715,7 +741,8 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
     NBG_CUDA(cudaLaunchKernelEx(&cfg, k_adj_step_umma, (const __nv_bfloat16 *)w_hi, (const __nv_bfloat16 *)w_lo,
                                 (const __nv_bfloat16 *)dI_hi_in, (const __nv_bfloat16 *)dI_lo_in,
                                 (__nv_bfloat16 *)dI_hi_out, (__nv_bfloat16 *)dI_lo_out, g_read, c_t, u, s, m, vprev,
-                                lam_v, dI, g_theta, g_alpha, alpha, theta, *p, N, err));
+                                lam_v, dI, g_theta, g_alpha, alpha, theta, *p, N, (__nv_bfloat16 *)dT_hi,
+                                (__nv_bfloat16 *)dT_lo, (long long)k_off, (long long)k_cols, err));
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }

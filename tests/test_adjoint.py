@@ -160,9 +160,11 @@ def test_graph_plan_backward_after_interleaved_forwards(record):
 def test_recorded_state_gradients_equal_replayed(graphs):
     """Recording every step's state in the forward and replaying segments
     from checkpoints in the backward run the same kernels on the same values:
-    the loss and all five gradients are bitwise equal.  T = 70 with segments
-    of 20 leaves a ragged last segment; N = 512 takes the fused tensor-core
-    adjoint step."""
+    the loss and the W_out, alpha and theta gradients are bitwise equal, and
+    W_in and W_rec (one product over the whole run with the record, one per
+    segment with the replay: other split-K sums) agree to FP32 rounding.
+    T = 70 with segments of 20 leaves a ragged last segment; N = 512 takes
+    the fused tensor-core adjoint step."""
     from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
 
     kw = dict(n_in=64, n_rec=512, n_out=5, checkpoint=20, seed=11)
@@ -170,8 +172,11 @@ def test_recorded_state_gradients_equal_replayed(graphs):
     labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
     out = [_grads(RecurrentLIF(record=r, use_graphs=graphs, **kw, **SPIKING), x, labels) for r in (False, True)]
     assert out[0][0] == out[1][0]
-    for a, b in zip(out[0][1], out[1][1]):
-        assert torch.equal(a, b)
+    for name, a, b in zip(("w_in", "w_rec", "w_out", "alpha", "theta"), out[0][1], out[1][1]):
+        if name in ("w_in", "w_rec"):
+            assert (a - b).abs().max().item() <= 1e-5 * a.abs().max().item(), name
+        else:
+            assert torch.equal(a, b), name
 
 
 def test_record_mode_default_follows_budget():
@@ -326,8 +331,8 @@ def test_fused_adjoint_step_equals_two_launch_form(monkeypatch, n_rec):
     from neuronbridge_gb300.adjoint import RecurrentLIF, poisson_inputs
 
     kw = dict(n_in=64, n_rec=n_rec, n_out=5, checkpoint=20, seed=11)
-    torch.manual_seed(0)
-    model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, **kw, **SPIKING)
+    torch.manual_seed(0)  # replay mode: both forms take the weight gradients per segment
+    model = RecurrentLIF(smooth=False, device="cuda", use_graphs=False, record=False, **kw, **SPIKING)
     rates = torch.linspace(5.0, 50.0, kw["n_in"]) * 8.0
     x = poisson_inputs(rates, T, 128, dt=1.0, seed=3)
     labels = torch.randint(0, kw["n_out"], (128,), generator=torch.Generator().manual_seed(6)).cuda()
