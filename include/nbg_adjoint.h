@@ -167,8 +167,10 @@ nbg_status nbg_adjoint_reduce_add(float *g, const float *part, int split, int64_
 
 /* C = A B for the readout's small products (B x N by N x O, its transposes):
  * element (r, c) of A at A[r * a_rs + c * a_cs], likewise B; C is M x N row
- * major.  One thread per output, the sum over k in ascending order in FP32, so
- * results do not depend on the launch.  No counterpart in the reference. */
+ * major, FP32 sums.  K < 64: one thread per output, k ascending; K >= 64: one
+ * warp per output, lane l adding k = l, l + 32, ... in order and the 32 lane
+ * sums added in a fixed tree.  The order depends only on K, so results do
+ * not depend on the launch.  No counterpart in the reference. */
 nbg_status nbg_small_gemm(const float *A, int a_rs, int a_cs, const float *B, int b_rs, int b_cs, float *C, int M,
                           int N, int K, void *stream);
 

@@ -339,19 +339,23 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         xT_hi = torch.empty(C256 * kk_max, device=dev, dtype=torch.bfloat16)
         xT_lo = torch.empty(C256 * kk_max, device=dev, dtype=torch.bfloat16)
 
-    def wgrad(s_rows, x_rows, L):
+    def transposes(s_rows, x_rows, L, stream):
+        """S^T and X^T of L steps in the products' blocked BF16 layout."""
+        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(s_rows), L, B, N, N256, _ptr(sT), None, stream))
+        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x_rows), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), stream))
+
+    def wgrad(L):
         """dW_rec += S^T dI and dW_in += X^T dI over L steps, dI^T in dT."""
         kk = L * B
-        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(s_rows), L, B, N, N256, _ptr(sT), None, st))
         ws = min(WGRAD_SPLIT, kk // 64)
         _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(sT), None, N, N256, kk, _ptr(w_part), ws,
                                          _ptr(tc_err), st))
         _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_rec), _ptr(w_part), ws, N * N, N256 * N, st))
         ws = min(WGRAD_IN_SPLIT, kk // 64)
-        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x_rows), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), st))
         _lib.check(lib.nbg_adjoint_wgrad(_ptr(dT_hi), _ptr(dT_lo), _ptr(xT_hi), _ptr(xT_lo), N, C256, kk,
                                          _ptr(w_part), ws, _ptr(tc_err), st))
         _lib.check(lib.nbg_adjoint_reduce_add(_ptr(g_w_in), _ptr(w_part), ws, C * N, C256 * N, st))
+
 
     segments = list(enumerate(range(0, T, K)))
     for seg, t0 in reversed(segments):
@@ -407,14 +411,16 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         if tc:
             if not fused:  # dI^T from the FP32 dI
                 _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, N, _ptr(dT_hi), _ptr(dT_lo), st))
-            wgrad(S, x[t0:t1], L)
+            transposes(S, x[t0:t1], L, st)
+            wgrad(L)
         else:
             g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
             g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
         if dI_next is not None:
             dI_next.copy_(dI[0])
     if whole:  # the whole run's weight gradients at once
-        wgrad(rec[1], x, T)
+        transposes(rec[1], x, T, st)
+        wgrad(T)
     return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), (tc_err if tc else None)
 
 

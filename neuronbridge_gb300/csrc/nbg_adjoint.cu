@@ -376,10 +376,15 @@ __global__ void k_poisson(float *__restrict__ x, const float *__restrict__ rates
 
 } // namespace
 
-// C[i][j] = sum over k, ascending, of A[i][k] B[k][j] (element (r, c) of A at
-// A[r * a_rs + c * a_cs], likewise B): one thread per output, sequential FP32
-// sums, so the result does not depend on the launch.  For the readout's small
-// products (B x N by N x O and the like).
+// C[i][j] = sum over k of A[i][k] B[k][j] (element (r, c) of A at
+// A[r * a_rs + c * a_cs], likewise B), for the readout's small products
+// (B x N by N x O and the like).  Short sums (K < kSmallGemmWarpK): one
+// thread per output, k ascending.  Long ones: one warp per output, lane l
+// adding k = l, l + 32, ... in order, then the 32 lane sums in a fixed tree.
+// Either way the order depends only on K, so the result does not depend on
+// the launch.
+constexpr int kSmallGemmWarpK = 64;
+
 __global__ void k_small_gemm(const float *__restrict__ A, int a_rs, int a_cs, const float *__restrict__ Bm, int b_rs,
                              int b_cs, float *__restrict__ Cm, int M, int N, int K) {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -390,14 +395,32 @@ __global__ void k_small_gemm(const float *__restrict__ A, int a_rs, int a_cs, co
     Cm[o] = acc;
 }
 
+__global__ void k_small_gemm_warp(const float *__restrict__ A, int a_rs, int a_cs, const float *__restrict__ Bm,
+                                  int b_rs, int b_cs, float *__restrict__ Cm, int M, int N, int K) {
+    const long long o = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (o >= (long long)M * N) return; // whole warps: o is the same for all 32 lanes
+    const int i = (int)(o / N), j = (int)(o % N);
+    float acc = 0.0f;
+    for (int k = lane; k < K; k += 32)
+        acc = acc + A[(size_t)i * a_rs + (size_t)k * a_cs] * Bm[(size_t)k * b_rs + (size_t)j * b_cs];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, d);
+    if (lane == 0) Cm[o] = acc;
+}
+
 extern "C" {
 
 nbg_status nbg_small_gemm(const float *A, int a_rs, int a_cs, const float *B, int b_rs, int b_cs, float *C, int M,
                           int N, int K, void *stream) {
     if (!A || !B || !C || M <= 0 || N <= 0 || K <= 0) return nbg_fail(NBG_ERR_INVALID, "nbg_small_gemm: bad arguments");
     const long long total = (long long)M * N;
-    k_small_gemm<<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)stream>>>(A, a_rs, a_cs, B, b_rs, b_cs, C, M,
-                                                                                   N, K);
+    if (K >= kSmallGemmWarpK)
+        k_small_gemm_warp<<<(unsigned)((total + 3) / 4), 128, 0, (cudaStream_t)stream>>>(A, a_rs, a_cs, B, b_rs, b_cs,
+                                                                                         C, M, N, K);
+    else
+        k_small_gemm<<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)stream>>>(A, a_rs, a_cs, B, b_rs, b_cs,
+                                                                                       C, M, N, K);
     NBG_CUDA(cudaGetLastError());
     return NBG_OK;
 }
