@@ -325,8 +325,9 @@ __device__ __forceinline__ Syn load_syn(const NetDev &n, int s) {
     return y;
 }
 
-// Bring synapse s's record into this SM's L1 ahead of its load (no
-// register, no wait).
+// Request synapse s's record ahead of its load (no register, no wait).  The
+// later load finds the line in L2 rather than in this SM's L1 (measured: about
+// 750 cycles instead of about 1,100 from DRAM, not the 40 of an L1 hit).
 template <class S>
 __device__ __forceinline__ void prefetch_syn(const NetDev &n, int s) {
     const void *p = S::plastic(n) ? (const void *)(n.rec + s) : (const void *)(n.wst + s);
@@ -377,8 +378,8 @@ constexpr int kPostChunk = 2;
 // [s, s1) of a spiking neuron, striding by the warp size.
 template <class S>
 __device__ __forceinline__ void post_stdp_lane(const NetDev &n, int s, int s1, int t) {
-    // every record of this lane's share into L1 first: the rounds after the
-    // first find theirs there
+    // every record of this lane's share requested first: the rounds after the
+    // first find theirs in L2
     for (int q = s + 32 * kPostChunk; q < s1; q += 32) prefetch_syn<S>(n, q);
     for (; s < s1; s += 32 * kPostChunk) {
         Syn y[kPostChunk];
@@ -475,13 +476,10 @@ constexpr int kBatch = 2;
 // order, for a neuron with arrivals at most steps: the records of up to
 // kBatch arrivals are loaded before any of them is applied (distinct
 // synapses, so no load depends on an earlier apply), one memory round trip
-// per round instead of one per arrival.  The synapse at CSC position gpos
-// (the neuron's generator input in a static network, else -1) comes from
-// registers.
+// per round instead of one per arrival.
 template <class S>
 __device__ __forceinline__ void apply_word_batched(const NetDev &n, const Model &M, NeuronRegs &r, float &acc_a,
-                                                   float &acc_b, bool gate, unsigned int word, int first, int t,
-                                                   int gpos, float gw, unsigned int gmeta) {
+                                                   float &acc_b, bool gate, unsigned int word, int first, int t) {
     while (word) {
         int sk[kBatch];
         Syn y[kBatch];
@@ -494,17 +492,8 @@ __device__ __forceinline__ void apply_word_batched(const NetDev &n, const Model 
             }
         }
 #pragma unroll
-        for (int k = 0; k < kBatch; ++k) {
-            if (sk[k] < 0) continue;
-            if (sk[k] == gpos) {
-                y[k].w = gw;
-                y[k].meta = gmeta;
-                y[k].apre = y[k].apost = y[k].wmax = y[k].a_pre = y[k].a_post = 0.0f;
-                y[k].last = 0;
-            } else {
-                y[k] = load_syn<S>(n, sk[k]);
-            }
-        }
+        for (int k = 0; k < kBatch; ++k)
+            if (sk[k] >= 0) y[k] = load_syn<S>(n, sk[k]);
 #pragma unroll
         for (int k = 0; k < kBatch; ++k)
             if (sk[k] >= 0) apply_loaded<S>(n, M, r, acc_a, acc_b, gate, sk[k], y[k], t);
@@ -684,8 +673,6 @@ constexpr int kGenCached = 1;
 struct GenIn {
     int local, delay, pos;
     float prob;
-    float w;           // static networks: the synapse's weight and meta,
-    unsigned int meta; // constant within a launch, so kept in registers
 };
 
 // Advance every neuron B steps (drain arrivals, integrate, compact spikes,
@@ -885,21 +872,12 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
         gin[q].delay = 0;
         gin[q].pos = 0;
         gin[q].prob = -1.0f; // never fires
-        gin[q].w = 0.0f;
-        gin[q].meta = 0u;
         if (active && g0 + q < g1) {
             gin[q].prob = generator_prob(n, n.gen_src[g0 + q], &gin[q].local);
             gin[q].delay = n.gen_delay[g0 + q];
             gin[q].pos = n.gen_pos[g0 + q];
-            if (!S::plastic(n)) { // static weights change only between run calls
-                const uint2 a = reinterpret_cast<const uint2 *>(n.wst)[base + gin[q].pos];
-                gin[q].w = __uint_as_float(a.x);
-                gin[q].meta = a.y;
-            }
         }
     }
-    // the generator input's CSC position when its record is in registers
-    const int gen_cached_pos = (!S::plastic(n) && active && g0 < g1) ? base + gin[0].pos : -1;
     // everything below reads or writes what the previous block's launch wrote
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // external spikes of the block's steps (InputSpike::ProcessEvent): one
@@ -942,19 +920,20 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
     // * Deep drain (S::deep): a pipeline three steps deep keeps the memory
     //   latency off the step.  At the top of step b the summary bits of step
     //   b + 3 and the first flagged mask word of step b + 2 are requested,
-    //   and the synapse records of the first arrivals of step b + 1 (whose
-    //   word arrived during step b - 1) are prefetched into L1, so that step
-    //   b + 1 finds them on the SM.  Further flagged words of a step (rare at a
-    //   few arrivals per hundred steps) are loaded when it runs.  The
-    //   requested words travel by asynchronous copy into shared memory and
+    //   and the synapse record of the first arrival of step b + 1 (whose word
+    //   arrived during step b - 1); the second arrival's record is requested
+    //   into the cache.  Further flagged words of a step (rare at a few
+    //   arrivals per hundred steps) are loaded when it runs.  The requested
+    //   words and record travel by asynchronous copy into shared memory and
     //   are read at the top of the next step: a load into a register would
     //   stall the step at its first use (the summary's shift, the move that
     //   rotates the pipeline), one memory round trip per step.
     // * Wide drain: the summary of step b + 3 (through shared memory, as
     //   above) and the first kWide flagged words of step b + 1 are requested
-    //   while step b runs, the records of
-    //   step b + 1's arrivals are prefetched into L1 at the end of step b,
-    //   and the arrivals of a word are applied kBatch per memory round trip.
+    //   while step b runs, and the arrivals of a word are applied kBatch per
+    //   memory round trip.  (Prefetching step b + 1's records at the end of
+    //   step b, and keeping the generator synapse's record in registers, both
+    //   made the static networks slower.)
     const bool fast = nw <= 32 && (g1 - g0) <= 32;
     const unsigned int D = (unsigned int)n.D;
     const unsigned int slot0 = (unsigned int)T0 % D; // the block's first slot; later ones by wrap_slot
@@ -1115,8 +1094,7 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
                         apply_word_staged<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t, pos_cur,
                                              s_rec + (((b + 1) & 1) * 256 + threadIdx.x) * 2, pos_nxt);
                     else
-                        apply_word_batched<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t, gen_cached_pos,
-                                              gin[0].w, gin[0].meta);
+                        apply_word_batched<S>(n, L, r, acc_a, acc_b, gate, word, base + wi * 32, t);
                 }
             } else {
                 int gq = g0;
@@ -1135,13 +1113,6 @@ __global__ void __launch_bounds__(256, S::min_blocks) k_update(const __grid_cons
             }
             spk = update_neuron<S>(n, L, r, acc_a, acc_b, noisy ? L.p[5] * gauss12(nkey, t) : 0.0f, j, t);
             if (tslot >= 0) n.trace[(size_t)(t - run_t0) * n.ntrace + tslot] = r.v;
-            if constexpr (!S::deep) {
-                if (fast && b + 1 < B) { // records of step b + 1's arrivals (its words have arrived) into L1
-#pragma unroll
-                    for (int k = 0; k < kWide; ++k)
-                        for (unsigned int m = w_cur[k]; m; m &= m - 1u) prefetch_syn<S>(n, base + k * 32 + __ffs(m) - 1);
-                }
-            }
         }
         if (spk) {
             pos_nxt = -1; // the post-synaptic pass below rewrites every record of this neuron
