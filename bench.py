@@ -63,7 +63,7 @@ BYTES_PER_POST_UPDATE = 36
 KUPDATE_TRAFFIC_BYTES = 30.39e6
 # DRAM bytes (read + write) of one k_update launch of the 256-instance batched
 # workload (15 steps), scaled from an ncu capture on its first 32 instances
-BATCHED_TRAFFIC_BYTES = 2.534e9  # 273.7 MB on 282,235 LIF neurons x 2,612,540 / 282,235 (256 x 15 launches)
+BATCHED_TRAFFIC_BYTES = 2.478e9  # 267.7 MB on 282,235 LIF neurons x 2,612,540 / 282,235 (256 x 15 launches)
 # DRAM bytes (read + write) of one dense step launch (64 x 8192, delivery and
 # update) from an ncu capture with a cold L2
 DENSE_TRAFFIC_BYTES = 277.5e6
