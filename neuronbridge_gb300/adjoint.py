@@ -11,15 +11,17 @@ RECORD_BUDGET_BYTES (13 bytes per neuron, row and step: 1.7 GB at
 T = 1000, B = 128, N = 1024), which takes the replay, a third of the
 backward, off the training step.
 
-* Spiking mode: the forward (and the backward's replay) runs each checkpoint
+* Spiking mode: the forward (and the backward's replay) runs each
   segment in one launch per row block: the input current of a step is the
   sum of the W_in rows of the row's nonzero inputs (x_t times the row) and
   the W_rec rows of its previous spikes, each in ascending order, so there
   is no GEMM in the forward at all.  The adjoint's recurrent term
   dI_{t+1} W_rec^T and the weight gradients run on tcgen05 in split BF16
-  (nbg_adjoint_tc.cu) where the shapes allow, else cuBLAS FP32.
+  (nbg_adjoint_tc.cu) where the shapes allow (B = 128, N a multiple of
+  128), else as the engine's FP32 CUDA-core product (nbg_small_gemm).
 * Smoothed (sigmoid) mode, the finite-difference test mode: x W_in and
-  s_{t-1} W_rec are cuBLAS FP32 GEMMs followed by the fused elementwise step.
+  s_{t-1} W_rec are that FP32 product too, followed by the fused elementwise
+  step.  No cuBLAS kernel runs in either mode.
 * All elementwise work of an adjoint step is one fused kernel.
 
 Readout: y_t = a_out y_{t-1} + s_t W_out, a_out = exp(-dt / tau_out), and
@@ -253,17 +255,25 @@ def _forward_body(lib, x, w_in, w_rec, w_out, alpha, theta, p, K, coef, ck_v, ck
                 lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, S[t0 + 1], None, U[t0], M[t0], VP[t0], z,
                                      coef_dev[t0:t1], alpha, theta, p, t1 - t0, B, N, st)
             continue
-        xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(t1 - t0, B, N)
+        xi = torch.empty((t1 - t0, B, N), device=x.device, dtype=torch.float32)
+        _gemm(lib, x[t0:t1], C, 1, w_in, N, 1, xi, (t1 - t0) * B, N, C, st)  # x W_in of the segment
         for t in range(t0, t1):
             if rec is None:
                 s, u_t, m_t, vp_t = sbuf[t & 1], None, None, None
             else:
                 s, u_t, m_t, vp_t = rec[1][t + 1], _ptr(rec[0][t]), _ptr(rec[2][t]), _ptr(rec[3][t])
-            torch.addmm(xi[t - t0], s_prev, w_rec, out=I)
+            _gemm(lib, s_prev, N, 1, w_rec, N, 1, I, B, N, N, st)  # s_{t-1} W_rec, then + x_t W_in
+            I.add_(xi[t - t0])
             _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(s), u_t, m_t, vp_t, _ptr(z),
                                                 float(coef[t]), _ptr(alpha), _ptr(theta), ctypes.byref(p), B, N, st))
             s_prev = s
     _readout(lib, z, w_out, out, st)
+
+
+def _gemm(lib, a, a_rs, a_cs, b, b_rs, b_cs, out, M, N, K, st) -> None:
+    """out (M x N, row-major) = A B with the engine's small deterministic
+    product; element (r, c) of A at a[r * a_rs + c * a_cs], likewise B."""
+    _lib.check(lib.nbg_small_gemm(_ptr(a), a_rs, a_cs, _ptr(b), b_rs, b_cs, _ptr(out), M, N, K, st))
 
 
 def _readout(lib, z, w_out, out, st) -> None:
@@ -312,6 +322,9 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
     # no transpose); the other forms keep dI in FP32
     dI = None if fused else torch.empty((L_max, B, N), device=dev, dtype=torch.float32)
     dI_next = None if fused else torch.empty((B, N), device=dev, dtype=torch.float32)
+    if not tc:  # the weight-gradient products of a segment (CUDA cores)
+        tmp_rec = torch.empty((N, N), device=dev, dtype=torch.float32)
+        tmp_in = torch.empty((C, N), device=dev, dtype=torch.float32)
     if tc:
         w_hi = torch.empty(N * N, device=dev, dtype=torch.bfloat16)
         w_lo = torch.empty(N * N, device=dev, dtype=torch.bfloat16)
@@ -371,9 +384,11 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                 lists.segment_gather(lib, x[t0:t1], w_in, w_rec, v, ref, S[1], None, U, M, VP, None, None, alpha,
                                      theta, p, L, B, N, st)
             else:
-                xi = (x[t0:t1].reshape(-1, C) @ w_in).reshape(L, B, N)
+                xi = torch.empty((L, B, N), device=dev, dtype=torch.float32)
+                _gemm(lib, x[t0:t1], C, 1, w_in, N, 1, xi, L * B, N, C, st)
                 for k in range(L):
-                    torch.addmm(xi[k], S[k], w_rec, out=I)
+                    _gemm(lib, S[k], N, 1, w_rec, N, 1, I, B, N, N, st)
+                    I.add_(xi[k])
                     _lib.check(lib.nbg_lif_forward_step(_ptr(I), _ptr(v), _ptr(ref), _ptr(S[k + 1]), _ptr(U[k]),
                                                         _ptr(M[k]), _ptr(VP[k]), None, 0.0, _ptr(alpha),
                                                         _ptr(theta), ctypes.byref(p), B, N, st))
@@ -399,7 +414,7 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
                 continue
             ge = None
             if have_next:  # dL/ds_t from the recurrent path: dI_{t+1} W_rec^T
-                torch.mm(dI_next if k == L - 1 else dI[k + 1], w_rec.t(), out=g_ext)
+                _gemm(lib, dI_next if k == L - 1 else dI[k + 1], N, 1, w_rec, 1, N, g_ext, B, N, N, st)
                 ge = g_ext
             _lib.check(lib.nbg_lif_adjoint_step(_ptr(ge), _ptr(g_read), float(coef[t]), _ptr(U[k]),
                                                 _ptr(S[k + 1]), _ptr(M[k]), _ptr(VP[k]), _ptr(lam_v),
@@ -414,8 +429,11 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
             transposes(S, x[t0:t1], L, st)
             wgrad(L)
         else:
-            g_w_rec.addmm_(S[:L].reshape(-1, N).t(), dI[:L].reshape(-1, N))
-            g_w_in.addmm_(x[t0:t1].reshape(-1, C).t(), dI[:L].reshape(-1, N))
+            # S^T dI and X^T dI over the segment's (step, row) pairs
+            _gemm(lib, S, 1, N, dI, N, 1, tmp_rec, N, N, L * B, st)
+            g_w_rec.add_(tmp_rec)
+            _gemm(lib, x[t0:t1], 1, C, dI, N, 1, tmp_in, C, N, L * B, st)
+            g_w_in.add_(tmp_in)
         if dI_next is not None:
             dI_next.copy_(dI[0])
     if whole:  # the whole run's weight gradients at once
@@ -464,7 +482,7 @@ class _GraphPlan:
     def _capture(fn):
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(side):  # warm-up: cuBLAS handles and workspaces exist before capture
+        with torch.cuda.stream(side):  # warm-up: allocations and library state exist before capture
             out = fn()
         torch.cuda.current_stream().wait_stream(side)
         g = torch.cuda.CUDAGraph()
