@@ -239,23 +239,28 @@ __global__ void __launch_bounds__(kThreads, 1)
 // the adjoint step t that consumes it.  Grid (N / 128, kAdjCluster) in
 // clusters of kAdjCluster CTAs along y: the CTAs of a cluster split the K
 // range of one 128-row tile of W exactly as k_adj_umma's split-K does
-// (cluster rank = split index), run the same three split products into
-// TMEM, and move their 128 x 128 partial into their own shared memory (the
-// drained pipeline stages), laid out [b][i].  After a cluster barrier, rank
-// r reduces batch rows [16 r, 16 r + 16) of the tile over the partials of
-// ranks 0..7 in order (read through distributed shared memory) -- the sum
-// k_lif_adj_split forms from g_parts, so the result is the same bit for bit
-// -- and runs the adjoint step on those elements, writing dI_t as the split
+// (cluster rank = split index) and run the same three split products into
+// TMEM.  Rank r owns batch rows [16 r, 16 r + 16) of the tile: every CTA
+// stores its partial of those rows straight into rank r's receive buffer
+// ([source rank][row][i], 64 KiB) through distributed shared memory, which
+// waits for nothing.  After one cluster barrier rank r adds the partials of
+// ranks 0..7 in order from its own shared memory -- the sum k_lif_adj_split
+// forms from g_parts, so the result is the same bit for bit -- and runs the
+// adjoint step on those elements, writing dI_t as the split
 // BF16 operand of the next step's product into the other of two buffers
 // (the next launch reads this one while writing its own), in FP32 (when dI
 // is given) and as the split BF16 operand of the weight gradients (when dT_hi
 // is given: dI^T, row i, column k_off + b of a k_cols-column blocked matrix,
-// eight consecutive b of one i per 16-byte store).  A
-// second cluster barrier keeps every CTA's shared memory alive until its
-// peers have read it.  Waits on mbarriers are bounded as in k_adj_umma; a
-// CTA that gives up still takes part in both cluster barriers, and the
-// error word marks the step's results invalid.
+// eight consecutive b of one i per 16-byte store).  No CTA reads another's
+// shared memory, so none waits for its peers before it exits.  Waits on
+// mbarriers are bounded as in k_adj_umma; a CTA that gives up still takes
+// part in the cluster barrier, and the error word marks the step's results
+// invalid.  Two pipeline stages (a CTA has two K chunks at N = 1024) leave
+// room for the receive buffer.
 constexpr int kAdjCluster = 8;
+constexpr int kAdjFusedStages = 2;
+constexpr int kAdjRecvBytes = kAdjN * kAdjM * 4;
+constexpr int kAdjFusedSmemBytes = kAdjFusedStages * kAdjStageBytes + kAdjRecvBytes + 1024 + 256;
 
 __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 1) k_adj_step_umma(
     const __nv_bfloat16 *__restrict__ w_hi, const __nv_bfloat16 *__restrict__ w_lo,
@@ -268,12 +273,12 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     long long k_off, long long k_cols, int *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *stages = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(stages + kAdjStages * kAdjStageBytes);
-    uint64_t *empty = full + kAdjStages;
-    uint64_t *done = empty + kAdjStages;
+    float *recv = reinterpret_cast<float *>(stages + kAdjFusedStages * kAdjStageBytes); // [rank][row][i]
+    uint64_t *full = (uint64_t *)((uint8_t *)recv + kAdjRecvBytes);
+    uint64_t *empty = full + kAdjFusedStages;
+    uint64_t *done = empty + kAdjFusedStages;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
-    float *part = reinterpret_cast<float *>(stages); // [b][i], 64 KiB, after the pipeline has drained
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t rank;
@@ -285,7 +290,7 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     const int iters = (ks == kAdjCluster - 1) ? kchunks - kc0 : per;
 
     if (threadIdx.x == 0) {
-        for (int st = 0; st < kAdjStages; ++st) {
+        for (int st = 0; st < kAdjFusedStages; ++st) {
             mbar_init(&full[st], 1);
             mbar_init(&empty[st], 1);
         }
@@ -309,7 +314,7 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     // previous step (which writes dI_{t+1}, lam_v and the gradients).
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (warp == 0 && lane == 0) { // producer
-        const int pre = iters < kAdjStages ? iters : kAdjStages;
+        const int pre = iters < kAdjFusedStages ? iters : kAdjFusedStages;
         for (int it = 0; it < pre; ++it) {
             uint8_t *st = stages + it * kAdjStageBytes;
             const size_t a_blk = (size_t)mt * kchunks + kc0 + it;
@@ -326,8 +331,8 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
                       kAdjBlockB, &full[it]);
         }
         for (int it = pre; it < iters; ++it) {
-            const int st_i = it % kAdjStages;
-            if (!mbar_wait(&empty[st_i], ((it / kAdjStages) & 1) ^ 1, abort)) break;
+            const int st_i = it % kAdjFusedStages;
+            if (!mbar_wait(&empty[st_i], ((it / kAdjFusedStages) & 1) ^ 1, abort)) break;
             uint8_t *st = stages + st_i * kAdjStageBytes;
             const int kc = kc0 + it;
             const size_t a_blk = (size_t)mt * kchunks + kc;
@@ -340,8 +345,8 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
         }
     } else if (warp == 1 && lane == 0) { // MMA issuer
         for (int it = 0; it < iters; ++it) {
-            const int st_i = it % kAdjStages;
-            if (!mbar_wait(&full[st_i], (it / kAdjStages) & 1, abort)) break;
+            const int st_i = it % kAdjFusedStages;
+            if (!mbar_wait(&full[st_i], (it / kAdjFusedStages) & 1, abort)) break;
             fence_after();
             const uint32_t a_hi = smem_addr(stages + st_i * kAdjStageBytes);
             const uint32_t a_lo = a_hi + kAdjBlockA;
@@ -383,40 +388,40 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
     mbar_wait(done, 0, abort);
     __syncthreads();
     fence_after();
-    // partial accumulator -> own shared memory, [b][i]: warp w holds rows
-    // i = 32 (w % 4) + lane and batch columns 64 (w / 4) + 16 c16 + c
+    // the partial accumulator to the rows' owners: warp w holds rows
+    // i = 32 (w % 4) + lane and batch columns b = 64 (w / 4) + 16 c16 + c,
+    // which rank 4 (w / 4) + c16 owns; they land in its receive buffer at
+    // [this rank][c][i]
     {
         const int q = warp & 3, h = warp >> 2;
         const int il = 32 * q + lane;
         if (!*abort) {
+            const uint32_t mine = smem_addr(recv) + (uint32_t)((ks * 16 * kAdjM + il) * 4);
 #pragma unroll
             for (int c16 = 0; c16 < 4; ++c16) {
                 float acc[16];
                 tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * h + 16 * c16), acc);
+                uint32_t ra;
+                asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(mine), "r"(4 * h + c16));
 #pragma unroll
-                for (int c = 0; c < 16; ++c) part[(64 * h + 16 * c16 + c) * kAdjM + il] = acc[c];
+                for (int c = 0; c < 16; ++c)
+                    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra + (uint32_t)(c * kAdjM * 4)), "f"(acc[c])
+                                 : "memory");
             }
         }
     }
     fence_before();
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-    // reduce batch rows [16 ks, 16 ks + 16) over the cluster's partials, in
-    // rank order, and run the adjoint step on them
+    // reduce this rank's batch rows over the cluster's partials, in rank
+    // order, and run the adjoint step on them
     {
-        const uint32_t local = smem_addr(part);
         // every partial of the thread's rows, loaded back to back, then added
         // in rank order
         float x[kRows][kAdjCluster];
 #pragma unroll
-        for (int k = 0; k < kRows; ++k) {
-            const uint32_t off = local + (uint32_t)(((16 * ks + 8 * bsub + k) * kAdjM + il) * 4);
+        for (int k = 0; k < kRows; ++k)
 #pragma unroll
-            for (int r = 0; r < kAdjCluster; ++r) {
-                uint32_t ra;
-                asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(off), "r"(r));
-                asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(x[k][r]) : "r"(ra));
-            }
-        }
+            for (int r = 0; r < kAdjCluster; ++r) x[k][r] = recv[(r * 16 + 8 * bsub + k) * kAdjM + il];
         uint32_t t_hi[kRows / 2], t_lo[kRows / 2]; // dI^T of the eight rows, split, packed in pairs
 #pragma unroll
         for (int k = 0; k < kRows; ++k) {
@@ -455,7 +460,6 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
             reinterpret_cast<uint4 *>(dT_lo + o)[0] = make_uint4(t_lo[0], t_lo[1], t_lo[2], t_lo[3]);
         }
     }
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
     if (threadIdx.x == 0 && *abort) atomicOr(err, kUmmaTimeout);
     if (warp == 2) {
         fence_after();
@@ -725,13 +729,14 @@ nbg_status nbg_lif_adjoint_step_fused(const void *w_hi, const void *w_lo, const 
                         "k_off + %d <= k_cols, k_cols a multiple of %d below 2^31", kAdjN, kAdjN, kKChunk);
     static bool attr_set = false;
     if (!attr_set) {
-        NBG_CUDA(cudaFuncSetAttribute(k_adj_step_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmemBytes));
+        NBG_CUDA(cudaFuncSetAttribute(k_adj_step_umma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kAdjFusedSmemBytes));
         attr_set = true;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(N / kAdjM, kAdjCluster);
     cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = kAdjSmemBytes;
+    cfg.dynamicSmemBytes = kAdjFusedSmemBytes;
     cfg.stream = (cudaStream_t)stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
