@@ -352,10 +352,10 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         xT_hi = torch.empty(C256 * kk_max, device=dev, dtype=torch.bfloat16)
         xT_lo = torch.empty(C256 * kk_max, device=dev, dtype=torch.bfloat16)
 
-    def transposes(s_rows, x_rows, L, stream):
+    def transposes(s_rows, x_rows, L):
         """S^T and X^T of L steps in the products' blocked BF16 layout."""
-        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(s_rows), L, B, N, N256, _ptr(sT), None, stream))
-        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x_rows), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), stream))
+        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(s_rows), L, B, N, N256, _ptr(sT), None, st))
+        _lib.check(lib.nbg_adjoint_blocked_t(_ptr(x_rows), L, B, C, C256, _ptr(xT_hi), _ptr(xT_lo), st))
 
     def wgrad(L):
         """dW_rec += S^T dI and dW_in += X^T dI over L steps, dI^T in dT."""
@@ -426,7 +426,7 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         if tc:
             if not fused:  # dI^T from the FP32 dI
                 _lib.check(lib.nbg_adjoint_blocked_t(_ptr(dI), L, B, N, N, _ptr(dT_hi), _ptr(dT_lo), st))
-            transposes(S, x[t0:t1], L, st)
+            transposes(S, x[t0:t1], L)
             wgrad(L)
         else:
             # S^T dI and X^T dI over the segment's (step, row) pairs
@@ -437,7 +437,7 @@ def _backward_body(lib, gy, x, w_in, w_rec, w_out, alpha, theta, z, ck_v, ck_ref
         if dI_next is not None:
             dI_next.copy_(dI[0])
     if whole:  # the whole run's weight gradients at once
-        transposes(rec[1], x, T, st)
+        transposes(rec[1], x, T)
         wgrad(T)
     return g_w_in, g_w_rec, g_w_out, g_alpha.sum(0), g_theta.sum(0), (tc_err if tc else None)
 
