@@ -363,10 +363,12 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
         commit(done);
     }
     __syncwarp();
-    asm volatile("griddepcontrol.wait;" ::: "memory"); // the previous step's writes are visible
     // this thread's share of the adjoint step: batch rows 16 ks + 8 bsub + k
     // of column i (eight consecutive rows: one 16-byte store of dI^T).  Its
-    // operands are loaded now, while the products run.
+    // operands are loaded while the products run: first those no adjoint
+    // step writes (the forward's record, g_read and the parameters, all
+    // complete before the first step of the sweep), before the wait for the
+    // previous step, then the accumulators that step updated.
     const int il = threadIdx.x & 127, bsub = threadIdx.x >> 7;
     const int i = mt * kAdjM + il;
     constexpr int kRows = 8;
@@ -377,14 +379,19 @@ __global__ void __cluster_dims__(1, kAdjCluster, 1) __launch_bounds__(kThreads, 
         const size_t idx = (size_t)(16 * ks + 8 * bsub + k) * n + i;
         op_u[k] = u[idx];
         op_s[k] = s[idx];
-        op_lv[k] = lam_v[idx];
         op_gr[k] = g_read[idx];
-        op_gt[k] = g_theta[idx];
-        op_ga[k] = g_alpha[idx];
         op_vp[k] = vprev[idx];
         op_m[k] = m[idx];
     }
     const float th = theta[i], al = alpha[i];
+    asm volatile("griddepcontrol.wait;" ::: "memory"); // the previous step's writes are visible
+#pragma unroll
+    for (int k = 0; k < kRows; ++k) {
+        const size_t idx = (size_t)(16 * ks + 8 * bsub + k) * n + i;
+        op_lv[k] = lam_v[idx];
+        op_gt[k] = g_theta[idx];
+        op_ga[k] = g_alpha[idx];
+    }
     mbar_wait(done, 0, abort);
     __syncthreads();
     fence_after();
